@@ -1,0 +1,424 @@
+"""Benchmark: Gsamples/s of forward+inverse DWT/MODWT on one large signal.
+
+Headline workload (one "step"): forward then inverse periodic DWT of one
+n = 2^26 signal (D4, J = 16, FP64 data, WC_F64_FAST arithmetic) with the
+signal already in HBM -- the roofline configuration of the wavecuda
+hot path.  The 512 MiB working buffers are larger than L2 (126 MB), so no L2
+flush is needed between steps.
+
+The JSON line also carries:
+  e2e          the same step through the reference-facing symbol
+               RgpuTransform (FWD then BWD) on pinned host buffers, host<->
+               device copies included;
+  roofline     the dominant kernel's algorithmic bytes per launch over its
+               live CUDA-event launch time, against the measured HBM peak;
+  cpu_baseline the oracle's CPU restatement of the reference path timed on
+               this host (1 core: the reference's dispatched CPU code is
+               serial), on a bounded sample of the same workload;
+  sweep        Gsamples/s and HBM fraction of every filter x {DWT, MODWT} x
+               precision at n = 2^26.
+
+``--impl reference`` times the reference's CPU implementation instead
+(oracle/_ref when it was built from the reference tree, else the oracle
+port) and prints the same metric with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gsamples/s fwd+inv DWT/MODWT (% HBM peak); batched CV smooths/s vs plain"
+FILTERS = {1: "Haar", 2: "D4", 3: "C6", 4: "LA8"}
+PREC = {0: "exact", 1: "fast", 2: "fp32"}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ multi-rank --
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return rank, ws
+
+
+class Dist:
+    """Barrier and max-over-ranks for torchrun launches (gloo on the host;
+    the benchmark runs independent replicas, one signal per GPU, with no
+    collective on the data path)."""
+
+    def __init__(self):
+        self.rank, self.world = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU arm --
+
+def cpu_time_dwt(n: int, filt: int, J: int, budget_s: float, use_ref: bool):
+    """Times fwd+inv DWT on the CPU (oracle port, or the reference's own
+    compiled sources when available) until budget_s has elapsed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    if not os.path.exists(pyoracle.ORACLE_SO):
+        pyoracle.build()
+    if use_ref and pyoracle.reference_available():
+        impl, kind = pyoracle.Reference(), "reference"
+    else:
+        impl, kind = pyoracle.Oracle(), "port"
+    from wavecuda_gb300 import signals
+    x = signals.roofline_input(n, seed=1)
+    reps, t_total = 0, 0.0
+    while t_total < budget_s or reps == 0:
+        t0 = time.perf_counter()
+        w = impl.dwt(x, J, filt)
+        impl.dwt(w, J, filt, 0)
+        t_total += time.perf_counter() - t0
+        reps += 1
+    return reps * n / t_total / 1e9, kind, reps, t_total
+
+
+# ---------------------------------------------------------------- GPU arm --
+
+def algorithmic_bytes(kernel: str, n: int, J: int, esize: int) -> float:
+    """Algorithmic HBM bytes of one launch of `kernel` at length n."""
+    if kernel.startswith("dwt_fwd_pass0") or kernel.startswith("dwt_inv_pass0"):
+        return 2.0 * n * esize      # read n, write n
+    if kernel.startswith("modwt_fwd_level"):
+        return 3.0 * n * esize      # read s_{l-1}, write s_l and d_l
+    if kernel.startswith("modwt_inv_level"):
+        return 3.0 * n * esize      # read s_l and d_l, write s_{l-1}
+    return 0.0
+
+
+def step_bytes(ttype: int, n: int, J: int, esize: int) -> float:
+    if ttype == 0:
+        return 4.0 * n * esize                         # fwd 2n + inv 2n
+    return ((1 + 2 * J) + (J + 2)) * n * esize         # fwd (1+2J)n + inv (J+2)n
+
+
+def run_gpu_step(wc, bufs, n, filt, ttype, J, prec, stream):
+    L = wc.lib()
+    x, w, r = bufs
+    if ttype == 0:
+        wc.check(L.wc_dwt_device(x.ptr, w.ptr, n, 1, J, filt, prec, stream))
+        wc.check(L.wc_dwt_device(w.ptr, r.ptr, n, 0, J, filt, prec, stream))
+    else:
+        wc.check(L.wc_modwt_device(x.ptr, w.ptr, n, 1, J, filt, prec, stream))
+        wc.check(L.wc_modwt_device(r.ptr, w.ptr, n, 0, J, filt, prec, stream))
+
+
+def time_gpu(wc, bufs, n, filt, ttype, J, prec, stream, steps, warmup, dist=None, profile=False):
+    import ctypes as C
+    L = wc.lib()
+    for _ in range(warmup):
+        run_gpu_step(wc, bufs, n, filt, ttype, J, prec, stream)
+    wc.check(L.wc_stream_synchronize(stream))
+    if dist:
+        dist.barrier()
+    e0, e1 = wc.Event(), wc.Event()
+    launches0 = wc.kernel_launch_count()
+    if profile:
+        L.wc_profile_start()
+    e0.record(stream)
+    for _ in range(steps):
+        run_gpu_step(wc, bufs, n, filt, ttype, J, prec, stream)
+    e1.record(stream)
+    wc.check(L.wc_stream_synchronize(stream))
+    prof = []
+    if profile:
+        arr = (KernelTime * 64)()
+        cnt = C.c_int()
+        L.wc_profile_stop(arr, 64, C.byref(cnt))
+        prof = [(arr[i].name.decode(), arr[i].launches, arr[i].total_ms) for i in range(cnt.value)]
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_ms(e1)
+    return ms, wc.kernel_launch_count() - launches0, prof
+
+
+def _kernel_time_struct():
+    import ctypes as C
+
+    class KT(C.Structure):
+        _fields_ = [("name", C.c_char * 64), ("launches", C.c_int64), ("total_ms", C.c_double)]
+    return KT
+
+
+KernelTime = None
+
+
+def ours(args):
+    global KernelTime
+    import ctypes as C
+    import wavecuda_gb300 as wc
+    from wavecuda_gb300 import signals
+    if not os.path.exists(wc.LIB_PATH):
+        from wavecuda_gb300 import build
+        build.build()
+    KernelTime = _kernel_time_struct()
+    L = wc.lib()
+    L.wc_profile_stop.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    dist = Dist()
+    n = 1 << args.log2n
+    filt, J, prec = args.filter, args.levels, args.precision
+    stream = wc.default_stream()
+    hbm, hbm_src = peaks()
+
+    maxJ_mod = 12
+    bufs = (wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n * 2 * maxJ_mod), wc.DeviceBuffer(8 * n))
+    x = signals.roofline_input(n, seed=1 + dist.rank)
+    bufs[0].upload(x)
+
+    clocks = ClockSampler()
+    clocks.start()
+    ms, launches, prof = time_gpu(wc, bufs, n, filt, 0, J, prec, stream, args.steps, args.warmup,
+                                  dist, profile=True)
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    value = args.steps * n * dist.world / (ms / 1e3) / 1e9
+
+    # correctness guard on the timed output: perfect reconstruction
+    r = bufs[2].download(np.float64, n)
+    pr_err = float(np.max(np.abs(r - x)) / np.max(np.abs(x)))
+
+    # dominant kernel and its live per-launch time
+    dom = max(prof, key=lambda p: p[2]) if prof else ("", 1, ms)
+    dom_bytes = algorithmic_bytes(dom[0], n, J, 8)
+    dom_avg_s = dom[2] / dom[1] / 1e3
+    achieved = dom_bytes / dom_avg_s / 1e9 if dom_bytes else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get(dom[0])
+    roofline = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": hbm,
+                "peak_source": hbm_src, "unit": "GB/s",
+                "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                "bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg_s * 1e3,
+                "step_frac": step_bytes(0, n, J, 8) * args.steps / (ms / 1e3) / 1e9 / hbm,
+                "kernels": [{"name": p[0], "launches": p[1], "total_ms": round(p[2], 4)}
+                            for p in prof]}
+
+    # e2e through the reference-facing symbol with pinned host buffers
+    hx = wc.HostBuffer(n)
+    hx.array[:] = x
+    L.wc_set_default_precision(prec)
+    len_c, sense_c, lev_c, tt_c = C.c_int(n), C.c_int(1), C.c_int(J), C.c_int(0)
+    f_c, fl_c = C.c_int(filt), C.c_int(wc.FILTER_LEN[filt])
+    dummy = np.zeros(1)
+    xp = C.cast(hx.ptr, C.POINTER(C.c_double))
+    dp = dummy.ctypes.data_as(C.POINTER(C.c_double))
+
+    def e2e_step():
+        sense_c.value = 1
+        L.RgpuTransform(xp, dp, C.byref(len_c), C.byref(sense_c), C.byref(lev_c),
+                        C.byref(tt_c), C.byref(f_c), C.byref(fl_c))
+        sense_c.value = 0
+        L.RgpuTransform(xp, dp, C.byref(len_c), C.byref(sense_c), C.byref(lev_c),
+                        C.byref(tt_c), C.byref(f_c), C.byref(fl_c))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = dist.max(time.perf_counter() - t0)
+    e2e_err = float(np.max(np.abs(hx.array - x)) / np.max(np.abs(x)))
+    e2e = {"value": args.steps * n * dist.world / t_e2e / 1e9, "unit": "Gsamples/s",
+           "h2d_bytes_per_step": 2 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,
+           "api": "RgpuTransform FWD+BWD, pinned host buffers", "pr_err": e2e_err}
+    hx.free()
+
+    out = {"metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": dist.world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: iid N(0,1) + 8 sinusoids, seeded",
+           "config": {"workload": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.log2n}, J={J}, "
+                                  f"FP64 data, {PREC[prec]} arithmetic",
+                      "n": n, "levels": J, "filter": FILTERS[filt], "precision": PREC[prec],
+                      "l2": "inputs (512 MiB) larger than L2; no flush",
+                      "parallelism": f"replicas x{dist.world}"},
+           "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+           "pr_err": pr_err}
+
+    if dist.rank == 0 and not args.no_cpu:
+        v, kind, reps, tt = cpu_time_dwt(1 << args.cpu_log2n, filt, min(J, args.cpu_log2n - 2),
+                                         args.cpu_budget, use_ref=False)
+        out["cpu_baseline"] = {"value": v, "unit": "Gsamples/s", "cores": 1, "kind": kind,
+                               "sample": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.cpu_log2n}, "
+                                         f"{reps} reps, {tt:.1f} s"}
+
+    if not args.no_sweep:
+        sweep = []
+        for ttype, Jt in ((0, J), (1, 12)):
+            for f in (1, 2, 3, 4):
+                for p in (1, 0, 2):
+                    if p == 2:
+                        xf = wc.DeviceBuffer(4 * n)
+                        # FP32 data: convert through a host round trip once
+                        xf.upload(x.astype(np.float32))
+                        fb = (xf, bufs[1], bufs[2])
+                    else:
+                        fb = bufs
+                    ms_s, _, _ = time_gpu(wc, fb, n, f, ttype, Jt, p, stream, args.sweep_steps, 1)
+                    esize = 4 if p == 2 else 8
+                    gs = args.sweep_steps * n / (ms_s / 1e3) / 1e9
+                    frac = step_bytes(ttype, n, Jt, esize) * args.sweep_steps / (ms_s / 1e3) / 1e9 / hbm
+                    sweep.append({"transform": "DWT" if ttype == 0 else "MODWT",
+                                  "filter": FILTERS[f], "J": Jt, "precision": PREC[p],
+                                  "gsamples_s": round(gs, 3), "hbm_frac": round(frac, 4),
+                                  "ms_per_step": round(ms_s / args.sweep_steps, 3)})
+                    if p == 2:
+                        xf.free()
+        out["sweep"] = sweep
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def reference(args):
+    rank, world = dist_env()
+    if rank != 0:
+        return
+    n = 1 << args.log2n
+    filt, J = args.filter, args.levels
+    # each step: one fwd+inv of the full n = 2^26 workload on the host
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    if not os.path.exists(pyoracle.ORACLE_SO):
+        pyoracle.build()
+    use_ref = pyoracle.reference_available()
+    impl = pyoracle.Reference() if use_ref else pyoracle.Oracle()
+    kind = "reference" if use_ref else "port"
+    from wavecuda_gb300 import signals
+    x = signals.roofline_input(n, seed=1)
+    for _ in range(args.warmup):
+        impl.dwt(impl.dwt(x, J, filt), J, filt, 0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        impl.dwt(impl.dwt(x, J, filt), J, filt, 0)
+    dt = time.perf_counter() - t0
+    v = args.steps * n / dt / 1e9
+    out = {"metric": METRIC, "value": v, "unit": "Gsamples/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: iid N(0,1) + 8 sinusoids, seeded", "impl": "reference",
+           "config": {"workload": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.log2n}, J={J}, FP64",
+                      "n": n, "levels": J, "filter": FILTERS[filt]},
+           "cpu_baseline": {"value": v, "unit": "Gsamples/s", "cores": 1, "kind": kind,
+                            "sample": f"full workload, {args.steps} steps; the reference's "
+                                      "dispatched CPU transform is serial"},
+           "e2e": {"value": v, "unit": "Gsamples/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--log2n", type=int, default=26)
+    ap.add_argument("--filter", type=int, default=2)
+    ap.add_argument("--levels", type=int, default=16)
+    ap.add_argument("--precision", type=int, default=1)
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-log2n", type=int, default=24)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

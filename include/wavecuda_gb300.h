@@ -1,0 +1,199 @@
+/*
+ * wavecuda_gb300 -- C ABI of the GB300 (sm_103a) wavelet library.
+ *
+ * Two layers:
+ *
+ *  1. The reference's own R-facing symbols, same names and signatures as
+ *     rfunctions.cuh:17-36 of the reference, so that the R package's
+ *     useDynLib(wavecuda, ...) bindings (NAMESPACE:26-30) resolve against this
+ *     library unchanged.  Every computation runs on the GPU: the Rcpu* symbols
+ *     are served by the same device path as the Rgpu* ones.
+ *
+ *  2. Status-returning entry points (wc_*): host-buffer calls, device-pointer
+ *     calls on a caller stream, batched smoothing, adjoints and small runtime
+ *     helpers.  Every wc_* call returns WC_OK (0) or an error code and never
+ *     exits the process; wc_last_error() describes the last failure.
+ *
+ * Codes (wvtheads.h:14-38, rfunctions.cuh:13-15 of the reference):
+ *   sense     FWD 1, BWD 0
+ *   filter    HAAR 1, D4 2, C6 3, LA8 4          (filterlen 2, 4, 6, 8)
+ *   ttype     DWT 0, MODWT (time ordered) 1
+ *   hardness  HARD 0, SOFT 1
+ *   threshtype MANUAL 0, UNIV 1, CV 2
+ *   levels are 0-based in C (R's min.level - 1).
+ *
+ * Layouts (haar.cpp:9-30, haar.cpp:561-585):
+ *   DWT   x (len values), transformed in place, interleaved: after J levels the
+ *         level-l details (1-based) sit at indices = 2^(l-1) mod 2^l and the
+ *         level-J scaling coefficients at indices = 0 mod 2^J.
+ *   MODWT xmod = [s_1 | d_1 | s_2 | d_2 | ... | s_J | d_J], 2*len*J values.
+ *
+ * Precision codes (wc_* calls; the R symbols use the process default):
+ *   WC_F64_EXACT  FP64, every product and sum rounded in the reference's order
+ *                 (no FMA contraction): results bit-identical to the
+ *                 reference CPU path.
+ *   WC_F64_FAST   FP64 data in HBM, arithmetic in double-float on the FP32
+ *                 pipes (about 2^-48 relative per operation).
+ *   WC_F32        FP32 data and arithmetic.
+ */
+#ifndef WAVECUDA_GB300_H
+#define WAVECUDA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define WC_API __attribute__((visibility("default")))
+#else
+#define WC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- status codes */
+#define WC_OK 0
+#define WC_ERR_ARG 1         /* invalid argument (length, code, pointer) */
+#define WC_ERR_LEVELS 2      /* level count or level range rejected */
+#define WC_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define WC_ERR_NOMEM 4       /* device or pinned host allocation failed */
+#define WC_ERR_UNSUPPORTED 5 /* combination not provided */
+#define WC_ERR_NODEVICE 6    /* no usable CUDA device */
+#define WC_ERR_TIMEOUT 7     /* a bounded device-side wait gave up */
+
+#define WC_F64_EXACT 0
+#define WC_F64_FAST 1
+#define WC_F32 2
+
+/* ------------------------------------------------- 1. reference symbols */
+
+/* rfunctions.cu:3 (RcpuTransform).  FWD DWT: x in place.  FWD MODWT: reads x,
+ * writes the first 2*len*J values of xmod.  BWD DWT: x in place.  BWD MODWT:
+ * reads xmod, writes x.  nlevels 0 means the maximum.  Errors are printed. */
+WC_API void RcpuTransform(double* x, double* xmod, int* len, int* sense, int* nlevels,
+                   int* ttype, int* filter, int* filterlen);
+
+/* rfunctions.cu:21 (RgpuTransform).  Same contract as RcpuTransform. */
+WC_API void RgpuTransform(double* x, double* xmod, int* len, int* sense, int* nlevels,
+                   int* ttype, int* filter, int* filterlen);
+
+/* rfunctions.cu:59 (RcpuThreshold).  Thresholds x (DWT) or xmod (MODWT) in
+ * place over levels [minlevel, maxlevel]. */
+WC_API void RcpuThreshold(double* x, double* xmod, int* len, int* nlevels, int* ttype,
+                   int* filter, int* filterlen, double* thresh, int* hardness,
+                   int* minlevel, int* maxlevel);
+
+/* rfunctions.cu:71 (RcpuSmooth).  Forward transform, threshold, inverse; x is
+ * replaced by the smoothed signal.  *thresh is input for MANUAL and receives
+ * the threshold used for UNIV and CV. */
+WC_API void RcpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filter,
+                int* filterlen, int* threshtype, double* thresh, int* hardness,
+                int* minlevel, int* maxlevel, double* tol);
+
+/* rfunctions.cu:102 (RgpuSmooth).  Same contract as RcpuSmooth; unlike the
+ * reference it also accepts UNIV and the D4/C6/LA8 filters. */
+WC_API void RgpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filter,
+                int* filterlen, int* threshtype, double* thresh, int* hardness,
+                int* minlevel, int* maxlevel, double* tol);
+
+/* ------------------------------------------------ 2. status-returning API */
+
+/* Text of the last error on this thread ("" when none). */
+WC_API const char* wc_last_error(void);
+
+/* Maximum level count for (len, filterlen): check_len_levels,
+ * wavutils.cpp:48-64 (0 when len is not a power of two >= filterlen). */
+WC_API int wc_max_levels(int64_t len, int filterlen);
+
+/* Process default precision used by the reference symbols (initially
+ * WC_F64_EXACT, or the WAVECUDA_PRECISION environment variable: "exact",
+ * "fast" or "fp32" -- fp32 converts at the boundary). */
+WC_API int wc_set_default_precision(int precision);
+WC_API int wc_get_default_precision(void);
+
+/* Host-buffer transform (replaces RgpuTransform, rfunctions.cu:21-56, with a
+ * status).  For WC_F32 the host data are still doubles; they are converted
+ * on the device. */
+WC_API int wc_transform(double* x, double* xmod, int64_t len, int sense, int nlevels,
+                 int ttype, int filter, int precision);
+
+/* Host-buffer threshold (replaces RcpuThreshold, rfunctions.cu:59-69). */
+WC_API int wc_threshold(double* x, double* xmod, int64_t len, int nlevels, int ttype,
+                 int filter, double thresh, int hardness, int minlevel,
+                 int maxlevel);
+
+/* Details of one smoothing call. */
+typedef struct {
+  double thresh;        /* threshold applied to the full transform */
+  double thresh_univ;   /* universal threshold (the CV bracket's upper end) */
+  int cv_iterations;    /* golden-section iterations (CV only) */
+  int levels;           /* level count used */
+  int64_t kept;         /* detail coefficients in [minlevel,maxlevel] kept */
+  int64_t zeroed;       /* ... and set to zero (|c| < thresh) */
+  double min_margin;    /* smallest |m1-m2|/m1 the search compared (CV) */
+} wc_smooth_info;
+
+/* Host-buffer smoothing (replaces RgpuSmooth/RcpuSmooth, rfunctions.cu:71-137,
+ * with a status).  info may be NULL. */
+WC_API int wc_smooth(double* x, int64_t len, int nlevels, int ttype, int filter,
+              int threshtype, double* thresh, int hardness, int minlevel,
+              int maxlevel, double tol, int precision, wc_smooth_info* info);
+
+/* ---- device-pointer API: inputs and outputs already in HBM.  stream is a
+ * cudaStream_t (NULL = the library's own stream).  Calls are asynchronous
+ * with respect to the host unless stated; scratch comes from the library's
+ * per-device workspace (grown on demand, kept until wc_release()). */
+
+/* DWT, out of place: in and out are distinct buffers of len elements (double
+ * for the FP64 precisions, float for WC_F32).  FWD: in = signal, out =
+ * interleaved transform.  BWD: in = interleaved transform, out = signal. */
+WC_API int wc_dwt_device(const void* in, void* out, int64_t len, int sense,
+                  int nlevels, int filter, int precision, void* stream);
+
+/* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
+ * BWD reads only s_J and d_1..d_J. */
+WC_API int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlevels,
+                    int filter, int precision, void* stream);
+
+/* Exact median and MAD (1.4826 * median |x - median|) of n FP64 values in
+ * device memory, as median()/mad() of utils.cpp:166-203 compute them (the
+ * two middle order statistics averaged).  Synchronous; results on the host. */
+WC_API int wc_median_mad_device(const double* data, int64_t n, double* median, double* mad,
+                                void* stream);
+
+/* ---- runtime helpers (device memory, pinned host memory, timing) */
+WC_API int wc_device_count(int* count);
+WC_API int wc_malloc_device(void** ptr, size_t bytes);
+WC_API int wc_free_device(void* ptr);
+WC_API int wc_malloc_host(void** ptr, size_t bytes); /* pinned */
+WC_API int wc_free_host(void* ptr);
+WC_API int wc_memcpy(void* dst, const void* src, size_t bytes, void* stream); /* any direction, async */
+WC_API int wc_memset_device(void* ptr, int value, size_t bytes, void* stream);
+WC_API int wc_stream_synchronize(void* stream);
+WC_API int wc_default_stream(void** stream);
+WC_API int wc_event_create(void** event);
+WC_API int wc_event_destroy(void* event);
+WC_API int wc_event_record(void* event, void* stream);
+WC_API int wc_event_elapsed_ms(void* start, void* stop, float* ms);
+/* Live per-kernel timing.  Between wc_profile_start() and wc_profile_stop()
+ * the library brackets each of its kernel launches with CUDA events on the
+ * launch's own stream; stop synchronises and returns, per kernel name, the
+ * number of launches and their summed device time. */
+typedef struct {
+  char name[64];
+  int64_t launches;
+  double total_ms;
+} wc_kernel_time;
+WC_API int wc_profile_start(void);
+WC_API int wc_profile_stop(wc_kernel_time* out, int capacity, int* count);
+
+/* Number of kernels this library launched in this process so far. */
+WC_API int64_t wc_kernel_launch_count(void);
+/* Frees the workspace, streams and events the library holds. */
+WC_API int wc_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

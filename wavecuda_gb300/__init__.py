@@ -1,0 +1,496 @@
+"""wavecuda_gb300: GB300-native (sm_103a) wavelet transforms, thresholding and
+cross-validated smoothing behind the wavecuda reference's C ABI.
+
+The compute lives in ``libwavecuda_gb300.so`` (CUDA kernels + C ABI, built
+in-tree by :mod:`wavecuda_gb300.build`).  This module binds it with ctypes and
+mirrors the reference's R entry points (R/rfunctions.R: CPUTransform,
+GPUTransform, CPUReconstruct, GPUReconstruct, CPUThreshold, CPUSmooth,
+GPUSmooth and their input checks) with the same argument meaning and the same
+error conditions (R's ``stop`` becomes ``ValueError``).  There is no CPU
+fallback: every call goes to the GPU library, and importing the bindings
+raises if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwavecuda_gb300.so")
+
+# Codes (wvtheads.h:14-38, rfunctions.cuh:13-15).
+FWD, BWD = 1, 0
+HAAR, D4, C6, LA8 = 1, 2, 3, 4
+DWT, MODWT = 0, 1
+HARD, SOFT = 0, 1
+MANUAL, UNIV, CV = 0, 1, 2
+F64_EXACT, F64_FAST, F32 = 0, 1, 2
+
+WC_OK = 0
+ERRORS = {1: "invalid argument", 2: "level error", 3: "CUDA error", 4: "out of memory",
+          5: "unsupported", 6: "no CUDA device", 7: "timeout"}
+
+FILTERS = {"Haar": HAAR, "D4": D4, "C6": C6, "LA8": LA8}
+FILTER_LEN = {HAAR: 2, D4: 4, C6: 6, LA8: 8}
+
+
+class WaveCudaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SmoothInfo(C.Structure):
+    _fields_ = [("thresh", C.c_double), ("thresh_univ", C.c_double),
+                ("cv_iterations", C.c_int), ("levels", C.c_int),
+                ("kept", C.c_int64), ("zeroed", C.c_int64), ("min_margin", C.c_double)]
+
+
+_lib: Optional[C.CDLL] = None
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+
+def lib() -> C.CDLL:
+    """The loaded GPU library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with python -m wavecuda_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    for name in ("RcpuTransform", "RgpuTransform"):
+        getattr(L, name).argtypes = [_dp, _dp] + [_ip] * 6
+        getattr(L, name).restype = None
+    L.RcpuThreshold.argtypes = [_dp, _dp] + [_ip] * 5 + [_dp, _ip, _ip, _ip]
+    L.RcpuThreshold.restype = None
+    for name in ("RcpuSmooth", "RgpuSmooth"):
+        getattr(L, name).argtypes = [_dp] + [_ip] * 6 + [_dp, _ip, _ip, _ip, _dp]
+        getattr(L, name).restype = None
+    L.wc_last_error.restype = C.c_char_p
+    L.wc_max_levels.argtypes = [C.c_int64, C.c_int]
+    L.wc_set_default_precision.argtypes = [C.c_int]
+    L.wc_transform.argtypes = [_dp, _dp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.wc_threshold.argtypes = [_dp, _dp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double,
+                               C.c_int, C.c_int, C.c_int]
+    L.wc_smooth.argtypes = [_dp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
+                            C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SmoothInfo)]
+    L.wc_dwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
+    L.wc_modwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
+    L.wc_median_mad_device.argtypes = [_vp, C.c_int64, _dp, _dp, _vp]
+    L.wc_device_count.argtypes = [_ip]
+    L.wc_malloc_device.argtypes = [C.POINTER(_vp), C.c_size_t]
+    L.wc_free_device.argtypes = [_vp]
+    L.wc_malloc_host.argtypes = [C.POINTER(_vp), C.c_size_t]
+    L.wc_free_host.argtypes = [_vp]
+    L.wc_memcpy.argtypes = [_vp, _vp, C.c_size_t, _vp]
+    L.wc_memset_device.argtypes = [_vp, C.c_int, C.c_size_t, _vp]
+    L.wc_stream_synchronize.argtypes = [_vp]
+    L.wc_default_stream.argtypes = [C.POINTER(_vp)]
+    L.wc_event_create.argtypes = [C.POINTER(_vp)]
+    L.wc_event_destroy.argtypes = [_vp]
+    L.wc_event_record.argtypes = [_vp, _vp]
+    L.wc_event_elapsed_ms.argtypes = [_vp, _vp, C.POINTER(C.c_float)]
+    L.wc_kernel_launch_count.restype = C.c_int64
+    _lib = L
+    return L
+
+
+def check(code: int) -> None:
+    if code != WC_OK:
+        raise WaveCudaError(code, lib().wc_last_error().decode())
+
+
+def last_error() -> str:
+    return lib().wc_last_error().decode()
+
+
+def _dptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _ci(v: int):
+    return C.byref(C.c_int(int(v)))
+
+
+# ------------------------------------------------------------------------
+# Mirror of R/rfunctions.R
+# ------------------------------------------------------------------------
+
+@dataclass
+class WST:
+    """The R "WST" object (return.trans, rfunctions.R:259-292)."""
+    x: np.ndarray
+    ttype: str
+    filt: str
+    filtlen: int
+    nlevels: int
+    len: int
+    w: np.ndarray
+
+
+def _ttype_code(transform_type):
+    return {"DWT": DWT, "MODWT": MODWT}.get(transform_type)
+
+
+def check_trans_inputs(xin, direction, nlevels, transform_type, filter):
+    """check.trans.inputs (rfunctions.R:64-119)."""
+    ttype = _ttype_code(transform_type)
+    if ttype is None:
+        raise ValueError("Unexpected transform type")
+    filt = FILTERS.get(filter)
+    if filt is None:
+        raise ValueError("Unexpected filter")
+    filtlen = FILTER_LEN[filt]
+    sense = {"FWD": FWD, "BWD": BWD}.get(direction)
+    if sense is None:
+        raise ValueError("Unexpected direction!")
+    xin = np.asarray(xin)
+    if not np.issubdtype(xin.dtype, np.number):
+        raise ValueError("Unexpected input vector")
+    lenxin = xin.size
+
+    def is_pow2(v):
+        return v > 0 and math.log2(v) == round(math.log2(v))
+
+    if ttype == DWT:
+        x = np.array(xin, dtype=np.float64)
+        xmod = np.zeros(0)
+        n = lenxin
+        if not is_pow2(n):
+            raise ValueError("Need length to be power of 2")
+    elif sense == FWD:
+        x = np.array(xin, dtype=np.float64)
+        n = lenxin
+        if not is_pow2(n):
+            raise ValueError("Need length to be power of 2")
+        xmod = np.zeros(int(n * 2 * math.log2(n)))
+    else:
+        xmod = np.array(xin, dtype=np.float64)
+        if nlevels == 0:
+            raise ValueError("Probably got an error of infinite length")
+        n = lenxin / (2 * nlevels)
+        if not is_pow2(n):
+            raise ValueError("Was this really a MODWT vector? If so, check nlevels. "
+                             "I calculate the reconstruction vector to be of inappropriate size.")
+        n = int(n)
+        x = np.zeros(n)
+    maxlevels = math.floor(math.log2(n / filtlen)) + 1 if n >= 1 else 0
+    if nlevels == 0:
+        nlevels = maxlevels
+    if nlevels != round(nlevels) or nlevels < 0 or nlevels > maxlevels:
+        raise ValueError(f"nlevels should be an integer [whole number] between 1 and {maxlevels}")
+    # The reference stops here for C6/LA8 MODWT (rfunctions.R:114-116); this
+    # library provides them, so the check is not repeated.
+    return dict(x=x, xmod=xmod, len=int(n), sense=sense, nlevels=int(nlevels), ttype=ttype,
+                filt=filt, filtlen=filtlen)
+
+
+def _call_transform(symbol, a):
+    xmod = a["xmod"] if a["xmod"].size else np.zeros(1)
+    getattr(lib(), symbol)(_dptr(a["x"]), _dptr(xmod), _ci(a["len"]), _ci(a["sense"]),
+                           _ci(a["nlevels"]), _ci(a["ttype"]), _ci(a["filt"]), _ci(a["filtlen"]))
+    err = last_error()
+    if err:
+        raise WaveCudaError(3, err)
+    a["xmod"] = xmod if a["xmod"].size else a["xmod"]
+    return a
+
+
+def _return_trans(a, transform_type, filter, xin):
+    if a["sense"] == FWD:
+        w = a["x"] if a["ttype"] == DWT else a["xmod"][: 2 * a["len"] * a["nlevels"]]
+        return WST(x=np.asarray(xin, dtype=np.float64), ttype=transform_type, filt=filter,
+                   filtlen=a["filtlen"], nlevels=a["nlevels"], len=a["len"], w=w)
+    return a["x"]
+
+
+def CPUTransform(xin, direction="FWD", nlevels=0, transform_type="DWT", filter="Haar"):
+    """CPUTransform (rfunctions.R:334-357); served by the GPU path."""
+    a = check_trans_inputs(xin, direction, nlevels, transform_type, filter)
+    return _return_trans(_call_transform("RcpuTransform", a), transform_type, filter, xin)
+
+
+def GPUTransform(xin, direction="FWD", nlevels=0, transform_type="DWT", filter="Haar"):
+    """GPUTransform (rfunctions.R:383-406)."""
+    a = check_trans_inputs(xin, direction, nlevels, transform_type, filter)
+    return _return_trans(_call_transform("RgpuTransform", a), transform_type, filter, xin)
+
+
+def _prepare_wst(xwav: WST):
+    """prepare.wst.arg.list (rfunctions.R:128-153)."""
+    ttype = _ttype_code(xwav.ttype)
+    filt = FILTERS[xwav.filt]
+    if ttype == DWT:
+        x, xmod = np.array(xwav.w, dtype=np.float64), np.zeros(0)
+    else:
+        x, xmod = np.zeros(xwav.len), np.array(xwav.w, dtype=np.float64)
+    return dict(x=x, xmod=xmod, len=xwav.len, sense=BWD, nlevels=xwav.nlevels, ttype=ttype,
+                filt=filt, filtlen=FILTER_LEN[filt])
+
+
+def CPUReconstruct(xwav: WST):
+    """CPUReconstruct (rfunctions.R:420-436)."""
+    return _call_transform("RcpuTransform", _prepare_wst(xwav))["x"]
+
+
+def GPUReconstruct(xwav: WST):
+    """GPUReconstruct (rfunctions.R:451-467)."""
+    return _call_transform("RgpuTransform", _prepare_wst(xwav))["x"]
+
+
+def check_thresh_inputs(xwav: WST, hard_soft, thresh, min_level, max_level):
+    """check.thresh.inputs (rfunctions.R:168-193)."""
+    a = _prepare_wst(xwav)
+    if np.ndim(thresh) != 0:
+        raise ValueError("Only scalar thresholds supported")
+    if thresh <= 0:
+        raise ValueError("Threshold must be greater than 0")
+    a["thresh"] = float(thresh)
+    a["hardness"] = {"hard": HARD, "soft": SOFT}.get(hard_soft)
+    if a["hardness"] is None:
+        raise ValueError("Only hard or soft thresholding supported")
+    if (min_level != round(min_level) or max_level != round(max_level) or min_level > max_level
+            or min_level <= 0 or max_level > xwav.nlevels):
+        raise ValueError("min.level and max.level must be integers in the range 1...nlevels")
+    a["min.level"] = int(min_level) - 1
+    a["max.level"] = int(max_level) - 1
+    return a
+
+
+def CPUThreshold(xwav: WST, thresh, hard_soft, min_level, max_level) -> WST:
+    """CPUThreshold (rfunctions.R:507-528)."""
+    a = check_thresh_inputs(xwav, hard_soft, thresh, min_level, max_level)
+    xmod = a["xmod"] if a["xmod"].size else np.zeros(1)
+    lib().RcpuThreshold(_dptr(a["x"]), _dptr(xmod), _ci(xwav.len), _ci(xwav.nlevels),
+                        _ci(a["ttype"]), _ci(a["filt"]), _ci(a["filtlen"]),
+                        C.byref(C.c_double(a["thresh"])), _ci(a["hardness"]),
+                        _ci(a["min.level"]), _ci(a["max.level"]))
+    err = last_error()
+    if err:
+        raise WaveCudaError(2, err)
+    out = WST(**{**xwav.__dict__})
+    out.w = a["x"] if a["ttype"] == DWT else xmod
+    return out
+
+
+def check_smooth_inputs(xin, nlevels, transform_type, filter, thresh_type, thresh, hard_soft,
+                        min_level, max_level, tol):
+    """check.smooth.inputs (rfunctions.R:211-249)."""
+    a = check_trans_inputs(xin, "FWD", nlevels, transform_type, filter)
+    a["threshtype"] = {"manual": MANUAL, "univ": UNIV, "cv": CV}.get(thresh_type)
+    if a["threshtype"] is None:
+        raise ValueError("Only manual, univ or cv supported for threshold type")
+    if thresh_type == "manual":
+        if thresh is None or np.ndim(thresh) != 0:
+            raise ValueError("Only scalar thresholds supported")
+        if thresh <= 0:
+            raise ValueError("Threshold must be greater than 0")
+        a["thresh"] = float(thresh)
+    else:
+        a["thresh"] = 0.0
+    if thresh_type == "cv":
+        if tol <= 0:
+            raise ValueError("Tolerance must be greater than 0")
+        a["tol"] = float(tol)
+    else:
+        a["tol"] = 0.0
+    a["hardness"] = {"hard": HARD, "soft": SOFT}.get(hard_soft)
+    if a["hardness"] is None:
+        raise ValueError("Only hard or soft thresholding supported")
+    if (min_level != round(min_level) or max_level != round(max_level) or min_level > max_level
+            or min_level <= 0 or max_level > nlevels):
+        raise ValueError("min.level and max.level must be integers in the range 1...nlevels")
+    a["min.level"] = int(min_level) - 1
+    a["max.level"] = int(max_level) - 1
+    return a
+
+
+def _call_smooth(symbol, a):
+    t = C.c_double(a["thresh"])
+    getattr(lib(), symbol)(_dptr(a["x"]), _ci(a["len"]), _ci(a["nlevels"]), _ci(a["ttype"]),
+                           _ci(a["filt"]), _ci(a["filtlen"]), _ci(a["threshtype"]), C.byref(t),
+                           _ci(a["hardness"]), _ci(a["min.level"]), _ci(a["max.level"]),
+                           C.byref(C.c_double(a["tol"])))
+    err = last_error()
+    if err:
+        raise WaveCudaError(3, err)
+    a["thresh"] = t.value
+    return a["x"]
+
+
+def CPUSmooth(xin, nlevels, transform_type, filter, thresh_type, thresh=None, hard_soft="soft",
+              min_level=1, max_level=1, tol=0.01):
+    """CPUSmooth (rfunctions.R:547-569)."""
+    a = check_smooth_inputs(xin, nlevels, transform_type, filter, thresh_type, thresh, hard_soft,
+                            min_level, max_level, tol)
+    return _call_smooth("RcpuSmooth", a)
+
+
+def GPUSmooth(xin, nlevels, transform_type, filter, thresh_type, thresh=None, hard_soft="soft",
+              min_level=1, max_level=1, tol=0.01):
+    """GPUSmooth (rfunctions.R:588-612).  Unlike the reference this accepts
+    "univ" and the D4/C6/LA8 filters (rfunctions.R:592-594 refused them)."""
+    a = check_smooth_inputs(xin, nlevels, transform_type, filter, thresh_type, thresh, hard_soft,
+                            min_level, max_level, tol)
+    return _call_smooth("RgpuSmooth", a)
+
+
+# ------------------------------------------------------------------------
+# Direct bindings of the status-returning API
+# ------------------------------------------------------------------------
+
+def max_levels(n: int, filt: int) -> int:
+    return lib().wc_max_levels(n, FILTER_LEN[filt])
+
+
+def set_default_precision(p: int) -> None:
+    check(lib().wc_set_default_precision(p))
+
+
+def transform(x, nlevels, ttype, filt, sense=FWD, precision=F64_EXACT, xmod=None):
+    """wc_transform on host arrays.  FWD DWT returns the interleaved transform,
+    FWD MODWT returns xmod, BWD returns the signal."""
+    L = lib()
+    if ttype == DWT:
+        y = np.array(x, dtype=np.float64, copy=True)
+        check(L.wc_transform(_dptr(y), None, y.size, sense, nlevels, ttype, filt, precision))
+        return y
+    if sense == FWD:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        J = nlevels or max_levels(x.size, filt)
+        xm = np.zeros(2 * J * x.size)
+        check(L.wc_transform(_dptr(x), _dptr(xm), x.size, FWD, J, ttype, filt, precision))
+        return xm
+    xm = np.ascontiguousarray(xmod if xmod is not None else x, dtype=np.float64)
+    n = xm.size // (2 * nlevels)
+    y = np.zeros(n)
+    check(L.wc_transform(_dptr(y), _dptr(xm), n, BWD, nlevels, ttype, filt, precision))
+    return y
+
+
+def threshold(w, n, nlevels, ttype, filt, thresh, hardness, minlevel, maxlevel):
+    y = np.array(w, dtype=np.float64, copy=True)
+    if ttype == DWT:
+        check(lib().wc_threshold(_dptr(y), None, n, nlevels, ttype, filt, thresh, hardness,
+                                 minlevel, maxlevel))
+    else:
+        check(lib().wc_threshold(None, _dptr(y), n, nlevels, ttype, filt, thresh, hardness,
+                                 minlevel, maxlevel))
+    return y
+
+
+def smooth(x, nlevels, ttype, filt, threshtype, thresh=0.0, hardness=SOFT, minlevel=0,
+           maxlevel=None, tol=1e-8, precision=F64_EXACT):
+    """wc_smooth: returns (smoothed, SmoothInfo)."""
+    y = np.array(x, dtype=np.float64, copy=True)
+    J = nlevels or max_levels(y.size, filt)
+    if maxlevel is None:
+        maxlevel = J - 1
+    t = C.c_double(thresh)
+    info = SmoothInfo()
+    check(lib().wc_smooth(_dptr(y), y.size, J, ttype, filt, threshtype, C.byref(t), hardness,
+                          minlevel, maxlevel, tol, precision, C.byref(info)))
+    return y, info
+
+
+def median_mad(v) -> tuple:
+    """Exact median and MAD of a host vector, computed on the device."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    buf = DeviceBuffer(max(8, v.nbytes))
+    buf.upload(v)
+    med, mad = C.c_double(), C.c_double()
+    check(lib().wc_median_mad_device(buf.ptr, v.size, C.byref(med), C.byref(mad), None))
+    buf.free()
+    return med.value, mad.value
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    lib().wc_device_count(C.byref(n))
+    return n.value
+
+
+def kernel_launch_count() -> int:
+    return lib().wc_kernel_launch_count()
+
+
+class DeviceBuffer:
+    """A device allocation made through the library (plumbing for tests and
+    the benchmark)."""
+
+    def __init__(self, nbytes: int):
+        p = _vp()
+        check(lib().wc_malloc_device(C.byref(p), nbytes))
+        self.ptr, self.nbytes = p.value, nbytes
+
+    def upload(self, a: np.ndarray, stream=None):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        check(lib().wc_memcpy(self.ptr, a.ctypes.data, a.nbytes, stream))
+        check(lib().wc_stream_synchronize(stream))
+
+    def download(self, dtype, count, stream=None) -> np.ndarray:
+        out = np.empty(count, dtype=dtype)
+        check(lib().wc_memcpy(out.ctypes.data, self.ptr, out.nbytes, stream))
+        check(lib().wc_stream_synchronize(stream))
+        return out
+
+    def free(self):
+        if self.ptr:
+            lib().wc_free_device(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class HostBuffer:
+    """Pinned host memory viewed as a numpy array."""
+
+    def __init__(self, count: int, dtype=np.float64):
+        dtype = np.dtype(dtype)
+        p = _vp()
+        check(lib().wc_malloc_host(C.byref(p), count * dtype.itemsize))
+        self.ptr = p.value
+        buf = (C.c_char * (count * dtype.itemsize)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=count)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            lib().wc_free_host(self.ptr)
+            self.ptr = None
+
+
+class Event:
+    def __init__(self):
+        p = _vp()
+        check(lib().wc_event_create(C.byref(p)))
+        self.ptr = p.value
+
+    def record(self, stream=None):
+        check(lib().wc_event_record(self.ptr, stream))
+
+    def elapsed_ms(self, other: "Event") -> float:
+        ms = C.c_float()
+        check(lib().wc_event_elapsed_ms(self.ptr, other.ptr, C.byref(ms)))
+        return ms.value
+
+
+def default_stream():
+    p = _vp()
+    check(lib().wc_default_stream(C.byref(p)))
+    return p.value

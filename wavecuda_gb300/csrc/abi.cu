@@ -1,0 +1,574 @@
+// C ABI of the library: the reference's R-facing symbols (rfunctions.cu:3-137)
+// and the status-returning wc_* entry points, plus the runtime they share:
+// per-thread error text, the per-device workspace and stream, and launch
+// accounting.  Every computation below goes to the device drivers; there is
+// no host compute path.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "wc_common.cuh"
+
+namespace wc {
+
+// ------------------------------------------------------------- errors ----
+
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+void clear_error() { g_err[0] = '\0'; }
+
+const char* last_error_text() { return g_err; }
+
+static std::atomic<int64_t> g_launches{0};
+
+void count_launches(int64_t k) { g_launches += k; }
+
+int after_launch(const char* what) {
+  g_launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(WC_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+  return WC_OK;
+}
+
+// ---------------------------------------------------------- profiling ----
+
+namespace {
+std::atomic<bool> g_prof{false};
+std::mutex g_prof_mu;
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+std::vector<ProfRec> g_prof_recs;
+std::vector<cudaEvent_t> g_event_pool;
+
+cudaEvent_t pool_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace
+
+LaunchTimer::LaunchTimer(const char* name, cudaStream_t s) : name_(name), s_(s), start_(nullptr) {
+  if (!g_prof.load(std::memory_order_relaxed)) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEvent_t e = pool_event();
+  cudaEventRecord(e, s_);
+  start_ = e;
+}
+
+LaunchTimer::~LaunchTimer() {
+  if (!start_) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  cudaEvent_t e = pool_event();
+  cudaEventRecord(e, s_);
+  g_prof_recs.push_back({name_, static_cast<cudaEvent_t>(start_), e});
+}
+
+// ---------------------------------------------------------- workspace ----
+
+namespace {
+
+struct DeviceState {
+  void* slot[kNumSlots] = {};
+  size_t size[kNumSlots] = {};
+  cudaStream_t stream = nullptr;
+};
+
+std::mutex g_mu;
+std::map<int, DeviceState> g_dev;
+thread_local int g_ws_err = WC_OK;
+
+DeviceState& state() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return g_dev[d];
+}
+
+}  // namespace
+
+void* workspace(Slot slot, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState& st = state();
+  if (bytes == 0) bytes = 256;
+  if (st.size[slot] >= bytes) return st.slot[slot];
+  if (st.slot[slot]) {
+    // Work queued on other streams may still use the old buffer.
+    cudaDeviceSynchronize();
+    cudaFree(st.slot[slot]);
+    st.slot[slot] = nullptr;
+    st.size[slot] = 0;
+  }
+  size_t grow = bytes + bytes / 8;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, grow);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&p, bytes);
+    grow = bytes;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    g_ws_err = fail(WC_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes,
+                    cudaGetErrorString(e));
+    return nullptr;
+  }
+  st.slot[slot] = p;
+  st.size[slot] = grow;
+  return p;
+}
+
+int workspace_error() { return g_ws_err == WC_OK ? WC_ERR_NOMEM : g_ws_err; }
+
+int ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(WC_ERR_NODEVICE, "no CUDA device available (%s)",
+                e != cudaSuccess ? cudaGetErrorString(e) : "count is 0");
+  }
+  return WC_OK;
+}
+
+cudaStream_t lib_stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState& st = state();
+  if (!st.stream) cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
+  return st.stream;
+}
+
+int check_levels(int64_t n, int nlevels, int filterlen) {
+  if (n <= 0 || (n & (n - 1)) != 0 || filterlen <= 0 || n < filterlen) return 0;
+  int maxlevels = 0;
+  while (((int64_t)filterlen << maxlevels) <= n) maxlevels++;  // floor(log2(n/L)) + 1
+  if (nlevels == 0) nlevels = maxlevels;
+  if (nlevels < 0 || nlevels > maxlevels) return 0;
+  return nlevels;
+}
+
+}  // namespace wc
+
+using namespace wc;
+
+namespace wc_abi {
+
+std::atomic<int> g_default_prec{-1};
+
+int default_prec() {
+  int p = g_default_prec.load();
+  if (p < 0) {
+    p = WC_F64_EXACT;
+    const char* e = getenv("WAVECUDA_PRECISION");
+    if (e) {
+      if (!strcmp(e, "fast")) p = WC_F64_FAST;
+      else if (!strcmp(e, "fp32")) p = WC_F32;
+    }
+    g_default_prec = p;
+  }
+  return p;
+}
+
+int check_codes(int64_t len, int ttype, int filter, int sense_or_0) {
+  if (filter < 1 || filter > 4) return fail(WC_ERR_ARG, "unrecognised filter %d", filter);
+  if (ttype != 0 && ttype != 1)
+    return fail(ttype == 2 ? WC_ERR_UNSUPPORTED : WC_ERR_ARG,
+                "transform type %d not provided (0 DWT, 1 time-ordered MODWT)", ttype);
+  if (sense_or_0 != 0 && sense_or_0 != 1) return fail(WC_ERR_ARG, "sense must be 1 (FWD) or 0 (BWD)");
+  if (len <= 0 || (len & (len - 1)) != 0) return fail(WC_ERR_ARG, "length %lld is not a power of 2", (long long)len);
+  return WC_OK;
+}
+
+cudaStream_t pick(void* stream) { return stream ? static_cast<cudaStream_t>(stream) : lib_stream(); }
+
+template <class A, class B>
+__global__ void convert_k(const A* __restrict__ in, B* __restrict__ out, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = (B)in[i];
+}
+
+template <class A, class B>
+int convert(const A* in, B* out, int64_t n, cudaStream_t s) {
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  convert_k<A, B><<<(unsigned)blocks, 256, 0, s>>>(in, out, n);
+  return after_launch("convert_k");
+}
+
+// Host-buffer transform: stage in HBM, run, copy back.
+int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels, int ttype,
+                   int filter, int filterlen, int prec) {
+  WC_TRY(ensure_device());
+  WC_TRY(check_codes(len, ttype, filter, sense));
+  if (filterlen != filter_len(filter))
+    return fail(WC_ERR_ARG, "filter length %d does not match filter %d", filterlen, filter);
+  const int J = check_levels(len, nlevels, filterlen);
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld and filter length %d",
+                          nlevels, (long long)len, filterlen);
+  if (prec < 0 || prec > 2) return fail(WC_ERR_ARG, "unknown precision %d", prec);
+  if (!x || (ttype == 1 && !xmod)) return fail(WC_ERR_ARG, "null data pointer");
+  cudaStream_t s = lib_stream();
+  const int64_t nx = len, nm = (ttype == 1) ? 2 * len * (int64_t)J : 0;
+  const size_t bx = sizeof(double) * (size_t)nx, bm = sizeof(double) * (size_t)nm;
+  double* A = static_cast<double*>(workspace(kSlotStageA, ttype == 1 ? bm : bx));
+  double* B = static_cast<double*>(workspace(kSlotStageB, bx));
+  if (!A || !B) return workspace_error();
+  float* fa = nullptr;
+  float* fb = nullptr;
+  if (prec == WC_F32) {
+    char* f = static_cast<char*>(workspace(kSlotConvert, sizeof(float) * (size_t)(nx + nm) + 512));
+    if (!f) return workspace_error();
+    fa = reinterpret_cast<float*>(f);
+    fb = reinterpret_cast<float*>(f + ((sizeof(float) * (size_t)(ttype == 1 ? nm : nx) + 255) / 256) * 256);
+  }
+  if (ttype == 0) {
+    WC_CUDA(cudaMemcpyAsync(A, x, bx, cudaMemcpyHostToDevice, s));
+    if (prec == WC_F32) {
+      WC_TRY(convert(A, fa, nx, s));
+      WC_TRY(dwt(fa, fb, len, sense, J, filter, prec, s));
+      WC_TRY(convert(fb, B, nx, s));
+    } else {
+      WC_TRY(dwt(A, B, len, sense, J, filter, prec, s));
+    }
+    WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
+  } else if (sense == 1) {
+    WC_CUDA(cudaMemcpyAsync(B, x, bx, cudaMemcpyHostToDevice, s));
+    if (prec == WC_F32) {
+      WC_TRY(convert(B, fb, nx, s));
+      WC_TRY(modwt(fb, fa, len, 1, J, filter, prec, s));
+      WC_TRY(convert(fa, A, nm, s));
+    } else {
+      WC_TRY(modwt(B, A, len, 1, J, filter, prec, s));
+    }
+    WC_CUDA(cudaMemcpyAsync(xmod, A, bm, cudaMemcpyDeviceToHost, s));
+  } else {
+    WC_CUDA(cudaMemcpyAsync(A, xmod, bm, cudaMemcpyHostToDevice, s));
+    if (prec == WC_F32) {
+      WC_TRY(convert(A, fa, nm, s));
+      WC_TRY(modwt(fb, fa, len, 0, J, filter, prec, s));
+      WC_TRY(convert(fb, B, nx, s));
+    } else {
+      WC_TRY(modwt(B, A, len, 0, J, filter, prec, s));
+    }
+    WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
+  }
+  WC_CUDA(cudaStreamSynchronize(s));
+  return WC_OK;
+}
+
+int threshold_host(double* x, double* xmod, int64_t len, int nlevels, int ttype, int filter,
+                   int filterlen, double t, int hardness, int minl, int maxl) {
+  WC_TRY(ensure_device());
+  WC_TRY(check_codes(len, ttype, filter, 0));
+  if (filterlen != filter_len(filter))
+    return fail(WC_ERR_ARG, "filter length %d does not match filter %d", filterlen, filter);
+  const int J = check_levels(len, nlevels, filterlen);
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
+  // threshold() (thresh.cpp:113-140) does nothing on a rejected level range.
+  if (minl < 0 || maxl < 0 || minl > maxl || maxl >= J)
+    return fail(WC_ERR_LEVELS, "min/max levels %d..%d must lie in 0..%d", minl, maxl, J - 1);
+  double* data = (ttype == 0) ? x : xmod;
+  if (!data) return fail(WC_ERR_ARG, "null data pointer");
+  const int64_t cnt = (ttype == 0) ? len : 2 * len * (int64_t)J;
+  const size_t b = sizeof(double) * (size_t)cnt;
+  cudaStream_t s = lib_stream();
+  double* A = static_cast<double*>(workspace(kSlotStageA, b));
+  if (!A) return workspace_error();
+  WC_CUDA(cudaMemcpyAsync(A, data, b, cudaMemcpyHostToDevice, s));
+  WC_TRY(wc::threshold(A, len, J, ttype, t, hardness, minl, maxl, WC_F64_EXACT, s));
+  WC_CUDA(cudaMemcpyAsync(data, A, b, cudaMemcpyDeviceToHost, s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  return WC_OK;
+}
+
+int smooth_host(double* x, int64_t len, int nlevels, int ttype, int filter, int filterlen,
+                int threshtype, double* thresh, int hardness, int minl, int maxl, double tol,
+                int prec, wc_smooth_info* info) {
+  WC_TRY(ensure_device());
+  WC_TRY(check_codes(len, ttype, filter, 0));
+  if (filterlen != filter_len(filter))
+    return fail(WC_ERR_ARG, "filter length %d does not match filter %d", filterlen, filter);
+  const int J = check_levels(len, nlevels, filterlen);
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
+  if (threshtype < 0 || threshtype > 2) return fail(WC_ERR_ARG, "unknown threshold type %d", threshtype);
+  if (prec < 0 || prec > 2) return fail(WC_ERR_ARG, "unknown precision %d", prec);
+  if (!x || !thresh) return fail(WC_ERR_ARG, "null pointer");
+  if (threshtype == 2 && !(tol > 0)) return fail(WC_ERR_ARG, "tolerance must be > 0");
+  cudaStream_t s = lib_stream();
+  const size_t b = sizeof(double) * (size_t)len;
+  double* A = static_cast<double*>(workspace(kSlotStageA, b));
+  if (!A) return workspace_error();
+  WC_CUDA(cudaMemcpyAsync(A, x, b, cudaMemcpyHostToDevice, s));
+  WC_TRY(wc::smooth(A, len, J, ttype, filter, threshtype, thresh, hardness, minl, maxl, tol, prec,
+                    s, info));
+  WC_CUDA(cudaMemcpyAsync(x, A, b, cudaMemcpyDeviceToHost, s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  return WC_OK;
+}
+
+void report(const char* who, int r) {
+  if (r != WC_OK) fprintf(stderr, "\n Error in %s: %s\n", who, wc::last_error_text());
+}
+
+}  // namespace wc_abi
+
+using namespace wc_abi;
+
+extern "C" {
+
+const char* wc_last_error(void) { return wc::last_error_text(); }
+
+int wc_max_levels(int64_t len, int filterlen) { return check_levels(len, 0, filterlen); }
+
+int wc_set_default_precision(int precision) {
+  if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
+  g_default_prec = precision;
+  return WC_OK;
+}
+
+int wc_get_default_precision(void) { return default_prec(); }
+
+// ---- reference symbols (rfunctions.cu) ----
+
+void RcpuTransform(double* x, double* xmod, int* len, int* sense, int* nlevels, int* ttype,
+                   int* filter, int* filterlen) {
+  clear_error();
+  report("transform", transform_host(x, xmod, *len, *sense, *nlevels, *ttype, *filter, *filterlen,
+                                     default_prec()));
+}
+
+void RgpuTransform(double* x, double* xmod, int* len, int* sense, int* nlevels, int* ttype,
+                   int* filter, int* filterlen) {
+  clear_error();
+  report("GPU transform", transform_host(x, xmod, *len, *sense, *nlevels, *ttype, *filter,
+                                         *filterlen, default_prec()));
+}
+
+void RcpuThreshold(double* x, double* xmod, int* len, int* nlevels, int* ttype, int* filter,
+                   int* filterlen, double* thresh, int* hardness, int* minlevel, int* maxlevel) {
+  clear_error();
+  report("threshold", threshold_host(x, xmod, *len, *nlevels, *ttype, *filter, *filterlen, *thresh,
+                                     *hardness, *minlevel, *maxlevel));
+}
+
+void RcpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filter, int* filterlen,
+                int* threshtype, double* thresh, int* hardness, int* minlevel, int* maxlevel,
+                double* tol) {
+  clear_error();
+  report("smooth", smooth_host(x, *len, *nlevels, *ttype, *filter, *filterlen, *threshtype, thresh,
+                               *hardness, *minlevel, *maxlevel, tol ? *tol : 0.0, default_prec(),
+                               nullptr));
+}
+
+void RgpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filter, int* filterlen,
+                int* threshtype, double* thresh, int* hardness, int* minlevel, int* maxlevel,
+                double* tol) {
+  clear_error();
+  report("GPU smooth", smooth_host(x, *len, *nlevels, *ttype, *filter, *filterlen, *threshtype,
+                                   thresh, *hardness, *minlevel, *maxlevel, tol ? *tol : 0.0,
+                                   default_prec(), nullptr));
+}
+
+// ---- status-returning host-buffer API ----
+
+int wc_transform(double* x, double* xmod, int64_t len, int sense, int nlevels, int ttype,
+                 int filter, int precision) {
+  clear_error();
+  return transform_host(x, xmod, len, sense, nlevels, ttype, filter, filter_len(filter), precision);
+}
+
+int wc_threshold(double* x, double* xmod, int64_t len, int nlevels, int ttype, int filter,
+                 double thresh, int hardness, int minlevel, int maxlevel) {
+  clear_error();
+  return threshold_host(x, xmod, len, nlevels, ttype, filter, filter_len(filter), thresh, hardness,
+                        minlevel, maxlevel);
+}
+
+int wc_smooth(double* x, int64_t len, int nlevels, int ttype, int filter, int threshtype,
+              double* thresh, int hardness, int minlevel, int maxlevel, double tol, int precision,
+              wc_smooth_info* info) {
+  clear_error();
+  return smooth_host(x, len, nlevels, ttype, filter, filter_len(filter), threshtype, thresh,
+                     hardness, minlevel, maxlevel, tol, precision, info);
+}
+
+// ---- device-pointer API ----
+
+int wc_dwt_device(const void* in, void* out, int64_t len, int sense, int nlevels, int filter,
+                  int precision, void* stream) {
+  clear_error();
+  WC_TRY(check_codes(len, 0, filter, sense));
+  const int J = check_levels(len, nlevels, filter_len(filter));
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
+  if (!in || !out || in == out) return fail(WC_ERR_ARG, "in and out must be distinct device buffers");
+  if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
+  return dwt(in, out, len, sense, J, filter, precision, pick(stream));
+}
+
+int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlevels, int filter,
+                    int precision, void* stream) {
+  clear_error();
+  WC_TRY(check_codes(len, 1, filter, sense));
+  const int J = check_levels(len, nlevels, filter_len(filter));
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
+  if (!x || !xmod) return fail(WC_ERR_ARG, "null device pointer");
+  if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
+  return modwt(x, xmod, len, sense, J, filter, precision, pick(stream));
+}
+
+int wc_median_mad_device(const double* data, int64_t n, double* median, double* mad,
+                         void* stream) {
+  clear_error();
+  if (!data || n <= 0 || !median || !mad) return fail(WC_ERR_ARG, "bad median/mad arguments");
+  SelectSource src{data, n, n, 1};
+  return median_mad(src, n, pick(stream), median, mad);
+}
+
+// ---- runtime helpers ----
+
+int wc_device_count(int* count) {
+  cudaError_t e = cudaGetDeviceCount(count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *count = 0;
+  }
+  return WC_OK;
+}
+
+int wc_malloc_device(void** ptr, size_t bytes) {
+  WC_CUDA(cudaMalloc(ptr, bytes));
+  return WC_OK;
+}
+int wc_free_device(void* ptr) {
+  WC_CUDA(cudaFree(ptr));
+  return WC_OK;
+}
+int wc_malloc_host(void** ptr, size_t bytes) {
+  WC_CUDA(cudaMallocHost(ptr, bytes));
+  return WC_OK;
+}
+int wc_free_host(void* ptr) {
+  WC_CUDA(cudaFreeHost(ptr));
+  return WC_OK;
+}
+int wc_memcpy(void* dst, const void* src, size_t bytes, void* stream) {
+  WC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, pick(stream)));
+  return WC_OK;
+}
+int wc_memset_device(void* ptr, int value, size_t bytes, void* stream) {
+  WC_CUDA(cudaMemsetAsync(ptr, value, bytes, pick(stream)));
+  return WC_OK;
+}
+int wc_stream_synchronize(void* stream) {
+  WC_CUDA(cudaStreamSynchronize(pick(stream)));
+  return WC_OK;
+}
+int wc_default_stream(void** stream) {
+  WC_TRY(ensure_device());
+  *stream = lib_stream();
+  return WC_OK;
+}
+int wc_event_create(void** event) {
+  cudaEvent_t e;
+  WC_CUDA(cudaEventCreate(&e));
+  *event = e;
+  return WC_OK;
+}
+int wc_event_destroy(void* event) {
+  WC_CUDA(cudaEventDestroy(static_cast<cudaEvent_t>(event)));
+  return WC_OK;
+}
+int wc_event_record(void* event, void* stream) {
+  WC_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(event), pick(stream)));
+  return WC_OK;
+}
+int wc_event_elapsed_ms(void* start, void* stop, float* ms) {
+  WC_CUDA(cudaEventElapsedTime(ms, static_cast<cudaEvent_t>(start), static_cast<cudaEvent_t>(stop)));
+  return WC_OK;
+}
+int64_t wc_kernel_launch_count(void) { return g_launches.load(); }
+
+int wc_profile_start(void) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (auto& r : g_prof_recs) {
+    g_event_pool.push_back(r.a);
+    g_event_pool.push_back(r.b);
+  }
+  g_prof_recs.clear();
+  g_prof = true;
+  return WC_OK;
+}
+
+int wc_profile_stop(wc_kernel_time* out, int capacity, int* count) {
+  g_prof = false;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  std::vector<wc_kernel_time> agg;
+  for (auto& r : g_prof_recs) {
+    cudaEventSynchronize(r.b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    size_t k = 0;
+    for (; k < agg.size(); k++)
+      if (!strncmp(agg[k].name, r.name, sizeof(agg[k].name) - 1)) break;
+    if (k == agg.size()) {
+      wc_kernel_time t{};
+      strncpy(t.name, r.name, sizeof(t.name) - 1);
+      agg.push_back(t);
+    }
+    agg[k].launches++;
+    agg[k].total_ms += ms;
+    g_event_pool.push_back(r.a);
+    g_event_pool.push_back(r.b);
+  }
+  g_prof_recs.clear();
+  int n = 0;
+  for (auto& t : agg) {
+    if (out && n < capacity) out[n] = t;
+    n++;
+  }
+  if (count) *count = n;
+  return WC_OK;
+}
+
+int wc_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (auto& kv : g_dev) {
+    cudaSetDevice(kv.first);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < kNumSlots; i++) {
+      if (kv.second.slot[i]) cudaFree(kv.second.slot[i]);
+      kv.second.slot[i] = nullptr;
+      kv.second.size[i] = 0;
+    }
+    if (kv.second.stream) cudaStreamDestroy(kv.second.stream);
+    kv.second.stream = nullptr;
+  }
+  cudaSetDevice(cur);
+  return WC_OK;
+}
+
+}  // extern "C"

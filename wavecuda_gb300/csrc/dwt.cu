@@ -1,0 +1,309 @@
+// Periodic DWT (Haar, D4, C6, LA8), forward and inverse, in the reference's
+// interleaved layout (haar.cpp:9-30) with the reference's convolution
+// alignment (daub4.cpp:20-88, c6.cpp:32-111, la8.cpp:27-115, haar.cpp:47-93).
+//
+// Design.  A transform of J levels runs as a few "passes"; a pass applies G
+// consecutive levels to a compact sequence y (length N) whose elements sit at
+// stride S in the interleaved array.  One CTA owns a tile of Tt consecutive
+// y values plus the periodic halo its G levels need, keeps every level's
+// intermediate in shared memory, assembles the tile's interleaved result in
+// shared memory and writes it back with one coalesced sweep.  The tile's
+// level-G scaling coefficients also go, compact, to a scratch array that the
+// next pass reads contiguously; the last pass handles the short coarse tail
+// in a single CTA.  The inverse runs the same passes in reverse order.
+//
+// Forward halo: a level-l scaling value at index k reads level l-1 values
+// 2k .. 2k+L-1, so G fused levels need H_0 = (L-2)(2^G - 1) values to the
+// right of the tile (computed redundantly; G is chosen per filter to keep
+// this near a tenth of the tile).  Inverse halo: an output pair q reads
+// (s,d)[q-j], j < L/2, so the left halo is need_l = ceil(need_{l-1}/2) + L/2-1
+// coefficients at level l.
+#include <algorithm>
+#include <vector>
+
+#include "wc_common.cuh"
+#include "wc_dd.cuh"
+
+namespace wc {
+namespace {
+
+constexpr int kThreads = 256;
+
+// Right halo of the forward pass at level l of G (in level-l values).
+__host__ __device__ constexpr int64_t fwd_halo(int L, int G, int l) {
+  return (int64_t)(L - 2) * (((int64_t)1 << (G - l)) - 1);
+}
+
+template <int F, class P>
+__device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V& s,
+                                         typename P::V& d) {
+  if constexpr (F == 1) {
+    s = haar_sum<P>(src[0], src[1]);
+    d = haar_dif<P>(src[0], src[1]);
+  } else {
+    constexpr int L = filter_len(F);
+    s = P::mul(src[0], tap_h(F, 0));
+    d = P::mul(src[0], tap_g(F, 0));
+#pragma unroll
+    for (int j = 1; j < L; j++) {
+      s = P::madd(s, src[j], tap_h(F, j));
+      d = P::madd(d, src[j], tap_g(F, j));
+    }
+  }
+}
+
+// Forward pass.  y[m] = in[m] (m < N, compact).  Writes the tile's
+// interleaved result to out[(t0+m)*S] and its level-G scaling values to
+// coarse[t0/2^G + k] (when coarse != nullptr).
+template <int F, class P>
+__global__ void __launch_bounds__(kThreads)
+dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
+             typename P::T* __restrict__ out, int64_t S,
+             typename P::T* __restrict__ coarse, int write_coarse_slots) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* A = reinterpret_cast<V*>(smem_raw);
+  const int64_t H0 = fwd_halo(L, G, 0);
+  V* B = A + (Tt + H0);
+  V* Z = B + (Tt / 2 + fwd_halo(L, G, 1));
+  const int64_t t0 = (int64_t)blockIdx.x * Tt;
+
+  for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+    A[m] = P::ld(in[wrap(t0 + m, N)]);
+  __syncthreads();
+
+  V* src = A;
+  V* dst = B;
+  for (int l = 1; l <= G; l++) {
+    const int64_t nD = Tt >> l;
+    const int64_t nS = nD + fwd_halo(L, G, l);
+    const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
+    for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+      V s, d;
+      fwd_pair<F, P>(src + 2 * k, s, d);
+      dst[k] = s;
+      if (k < nD) Z[doff + k * dstep] = d;
+    }
+    __syncthreads();
+    V* t = src; src = dst; dst = t;
+  }
+  const int64_t nC = Tt >> G;
+  for (int64_t k = threadIdx.x; k < nC; k += blockDim.x) {
+    Z[k << G] = src[k];
+    if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
+  }
+  __syncthreads();
+  const int64_t cmask = ((int64_t)1 << G) - 1;
+  for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+    if (write_coarse_slots || (m & cmask) != 0) out[(t0 + m) * S] = P::st(Z[m]);
+  }
+}
+
+// Inverse pass: reconstructs y[t0 .. t0+Tt) of the compact level sequence
+// (length N) from the level-G scaling values (coarse, length N/2^G, stride
+// cstride) and the details of levels 1..G stored at det[m*S] (m = 2^(l-1) mod
+// 2^l).  Writes outp[(t0+m)*ostride].
+struct InvGeom {
+  int need[24];  // left halo at level l (coefficients)
+  int off[24];   // buffer offset of level l
+};
+
+template <int F, class P>
+__global__ void __launch_bounds__(kThreads)
+dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
+             const typename P::T* __restrict__ det, int64_t S, int64_t N, int G,
+             int64_t Tt, typename P::T* __restrict__ outp, int64_t ostride,
+             InvGeom geo) {
+  using V = typename P::V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t H = (int64_t)geo.need[G] << G;  // left halo of the staged array
+  V* Z = reinterpret_cast<V*>(smem_raw);
+  V* SA = Z + (Tt + H);
+  V* SB = SA + (Tt + 2 * geo.off[0] + 16);
+  const int64_t t0 = (int64_t)blockIdx.x * Tt;
+
+  for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+    Z[m] = P::ld(det[wrap(t0 - H + m, N) * S]);
+  {
+    const int64_t NG = N >> G, q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
+    V* buf = (G & 1) ? SB : SA;  // level-G buffer; level 0 ends in SA
+    for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
+      buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG) * cstride]);
+  }
+  __syncthreads();
+
+  for (int l = G; l >= 1; l--) {
+    V* src = (l & 1) ? SB : SA;
+    V* dst = (l & 1) ? SA : SB;
+    const int P_l = (geo.need[l - 1] + 1) >> 1;
+    const int64_t nq = (Tt >> l) + P_l;
+    const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
+    for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
+      const int64_t qr = k - P_l;  // q - q0
+      constexpr int HH = filter_len(F) / 2;
+      V sv[HH], dv[HH];
+#pragma unroll
+      for (int j = 0; j < HH; j++) {
+        sv[j] = src[qr - j + geo.off[l]];
+        dv[j] = Z[(qr - j) * dstep + doff];
+      }
+      V e, o;
+      // inv_pair addresses s[-j] / d[-j]; sv/dv are stored in ascending j.
+      if constexpr (F == 1) {
+        e = haar_sum<P>(sv[0], dv[0]);
+        o = haar_dif<P>(sv[0], dv[0]);
+      } else {
+        e = P::mul(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+        o = P::mul(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+        e = P::madd(e, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+        o = P::madd(o, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+        for (int j = HH - 2; j >= 0; j--) {
+          e = P::madd(e, sv[j], tap_h(F, 2 * j));
+          o = P::madd(o, sv[j], tap_h(F, 2 * j + 1));
+          e = P::madd(e, dv[j], tap_g(F, 2 * j));
+          o = P::madd(o, dv[j], tap_g(F, 2 * j + 1));
+        }
+      }
+      dst[2 * qr + geo.off[l - 1]] = e;
+      dst[2 * qr + 1 + geo.off[l - 1]] = o;
+    }
+    __syncthreads();
+  }
+  for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x)
+    outp[(t0 + m) * ostride] = P::st(SA[m + geo.off[0]]);
+}
+
+struct PassPlan {
+  int64_t N, S, Tt;
+  int G;
+};
+
+constexpr size_t kSmemBudget = 100 * 1024;
+
+template <class P>
+size_t fwd_smem(int L, int G, int64_t Tt) {
+  return sizeof(typename P::V) * (size_t)(Tt + fwd_halo(L, G, 0) + Tt / 2 +
+                                          fwd_halo(L, G, 1) + Tt);
+}
+
+InvGeom inv_geom(int L, int G) {
+  InvGeom g{};
+  g.need[0] = 0;
+  for (int l = 1; l <= G; l++) g.need[l] = (g.need[l - 1] + 1) / 2 + L / 2 - 1;
+  g.off[G] = g.need[G];
+  for (int l = 0; l < G; l++) g.off[l] = 2 * ((g.need[l] + 1) / 2);
+  return g;
+}
+
+template <class P>
+size_t inv_smem(int L, int G, int64_t Tt) {
+  InvGeom g = inv_geom(L, G);
+  int64_t H = (int64_t)g.need[G] << G;
+  return sizeof(typename P::V) * (size_t)((Tt + H) + 2 * (Tt + 2 * g.off[0] + 16));
+}
+
+template <class P>
+std::vector<PassPlan> plan_passes(int64_t n, int J, int F) {
+  const int L = filter_len(F);
+  const int64_t TT = (int64_t)(4096 * 8 / sizeof(typename P::V));
+  const int gmax = F == 1 ? 30 : F == 2 ? 8 : F == 3 ? 7 : 6;
+  std::vector<PassPlan> plan;
+  int64_t N = n, S = 1;
+  int l = 0;
+  while (l < J) {
+    const int64_t Tt = std::min(N, TT);
+    int G = std::min(J - l, (Tt == N) ? 30 : gmax);
+    while ((((int64_t)1 << G) > Tt) ||
+           fwd_smem<P>(L, G, Tt) > kSmemBudget || inv_smem<P>(L, G, Tt) > kSmemBudget)
+      G--;
+    plan.push_back({N, S, Tt, G});
+    N >>= G;
+    S <<= G;
+    l += G;
+  }
+  return plan;
+}
+
+template <int F, class P>
+int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream_t s) {
+  using T = typename P::T;
+  const int L = filter_len(F);
+  const T* in = static_cast<const T*>(vin);
+  T* out = static_cast<T*>(vout);
+  std::vector<PassPlan> plan = plan_passes<P>(n, J, F);
+  const int np = (int)plan.size();
+  T* scratch[2] = {nullptr, nullptr};
+  if (np > 1) {
+    size_t cbytes = sizeof(T) * (size_t)(plan[0].N >> plan[0].G);
+    scratch[0] = static_cast<T*>(workspace(kSlotCoarse0, cbytes));
+    scratch[1] = static_cast<T*>(workspace(kSlotCoarse1, cbytes));
+    if (!scratch[0] || !scratch[1]) return workspace_error();
+  }
+  if (sense == 1) {
+    const T* src = in;
+    for (int p = 0; p < np; p++) {
+      const PassPlan& pp = plan[p];
+      const bool last = (p == np - 1);
+      T* coarse = last ? nullptr : scratch[p & 1];
+      size_t smem = fwd_smem<P>(L, pp.G, pp.Tt);
+      auto kern = dwt_fwd_pass<F, P>;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      {
+        LaunchTimer lt(p == 0 ? "dwt_fwd_pass0" : "dwt_fwd_pass", s);
+        kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, pp.S,
+                                                             coarse, (last || pp.S == 1) ? 1 : 0);
+      }
+      WC_TRY(after_launch("dwt_fwd_pass"));
+      src = coarse;
+    }
+  } else {
+    // Passes in reverse order; pass p reads its coarse input from the
+    // interleaved array (top pass) or from the scratch written by pass p+1.
+    const T* coarse = in;
+    int64_t cstride = plan[np - 1].S << plan[np - 1].G;
+    for (int p = np - 1; p >= 0; p--) {
+      const PassPlan& pp = plan[p];
+      T* dst = (p == 0) ? out : scratch[p & 1];
+      InvGeom geo = inv_geom(L, pp.G);
+      size_t smem = inv_smem<P>(L, pp.G, pp.Tt);
+      auto kern = dwt_inv_pass<F, P>;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      {
+        LaunchTimer lt(p == 0 ? "dwt_inv_pass0" : "dwt_inv_pass", s);
+        kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(coarse, cstride, in, pp.S, pp.N,
+                                                             pp.G, pp.Tt, dst, 1, geo);
+      }
+      WC_TRY(after_launch("dwt_inv_pass"));
+      coarse = dst;
+      cstride = 1;
+    }
+  }
+  return WC_OK;
+}
+
+template <class P>
+int dispatch_dwt(const void* in, void* out, int64_t n, int sense, int J, int F, cudaStream_t s) {
+  switch (F) {
+    case 1: return run_dwt<1, P>(in, out, n, sense, J, s);
+    case 2: return run_dwt<2, P>(in, out, n, sense, J, s);
+    case 3: return run_dwt<3, P>(in, out, n, sense, J, s);
+    case 4: return run_dwt<4, P>(in, out, n, sense, J, s);
+  }
+  return fail(WC_ERR_ARG, "unknown filter %d", F);
+}
+
+}  // namespace
+
+int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
+        cudaStream_t s) {
+  switch (prec) {
+    case WC_F64_EXACT: return dispatch_dwt<PExact>(in, out, n, sense, J, F, s);
+    case WC_F64_FAST: return dispatch_dwt<PDD>(in, out, n, sense, J, F, s);
+    case WC_F32: return dispatch_dwt<PF32>(in, out, n, sense, J, F, s);
+  }
+  return fail(WC_ERR_ARG, "unknown precision %d", prec);
+}
+
+}  // namespace wc
