@@ -162,6 +162,12 @@ WC_API int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlev
 WC_API int wc_median_mad_device(const double* data, int64_t n, double* median, double* mad,
                                 void* stream);
 
+/* ((0 + v[0]) + v[1]) + ... + v[n-1], every addition rounded as a serial
+ * FP64 loop rounds it, for n non-negative FP64 terms in device memory
+ * (the summation of the cross-validation loss, thresh.cpp:363-383).
+ * Computed in parallel; synchronous; the sum is returned on the host. */
+WC_API int wc_sequential_sum_device(const double* terms, int64_t n, double* sum, void* stream);
+
 /* ---- runtime helpers (device memory, pinned host memory, timing) */
 WC_API int wc_device_count(int* count);
 WC_API int wc_malloc_device(void** ptr, size_t bytes);

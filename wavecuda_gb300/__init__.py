@@ -84,6 +84,7 @@ def lib() -> C.CDLL:
     L.wc_dwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
     L.wc_modwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
     L.wc_median_mad_device.argtypes = [_vp, C.c_int64, _dp, _dp, _vp]
+    L.wc_sequential_sum_device.argtypes = [_vp, C.c_int64, _dp, _vp]
     L.wc_device_count.argtypes = [_ip]
     L.wc_malloc_device.argtypes = [C.POINTER(_vp), C.c_size_t]
     L.wc_free_device.argtypes = [_vp]
@@ -412,6 +413,17 @@ def median_mad(v) -> tuple:
     check(lib().wc_median_mad_device(buf.ptr, v.size, C.byref(med), C.byref(mad), None))
     buf.free()
     return med.value, mad.value
+
+
+def sequential_sum(v) -> float:
+    """Serial-order FP64 sum of non-negative terms, computed on the device."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    buf = DeviceBuffer(max(8, v.nbytes))
+    buf.upload(v)
+    out = C.c_double()
+    check(lib().wc_sequential_sum_device(buf.ptr, v.size, C.byref(out), None))
+    buf.free()
+    return out.value
 
 
 def device_count() -> int:

@@ -19,6 +19,10 @@
 
 namespace wc {
 
+int cv_sequential_sum(const double* terms, int64_t count, double* dev_out, void* scratch,
+                      cudaStream_t s);
+size_t cv_sum_scratch_bytes(int64_t count);
+
 // ------------------------------------------------------------- errors ----
 
 static thread_local char g_err[512] = "";
@@ -444,6 +448,21 @@ int wc_median_mad_device(const double* data, int64_t n, double* median, double* 
   if (!data || n <= 0 || !median || !mad) return fail(WC_ERR_ARG, "bad median/mad arguments");
   SelectSource src{data, n, n, 1};
   return median_mad(src, n, pick(stream), median, mad);
+}
+
+int wc_sequential_sum_device(const double* terms, int64_t n, double* sum, void* stream) {
+  clear_error();
+  if (!terms || n <= 0 || !sum) return fail(WC_ERR_ARG, "bad sequential-sum arguments");
+  cudaStream_t s = pick(stream);
+  char* scr = static_cast<char*>(workspace(kSlotReduce, cv_sum_scratch_bytes(n) + 256));
+  if (!scr) return workspace_error();
+  double* dout = reinterpret_cast<double*>(scr);
+  WC_TRY(cv_sequential_sum(terms, n, dout, scr + 256, s));
+  double h = 0.0;
+  WC_CUDA(cudaMemcpyAsync(&h, dout, sizeof(double), cudaMemcpyDeviceToHost, s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  *sum = 2.0 * h;  // the kernel returns m * 0.5 (interp_mse); undo the exact halving
+  return WC_OK;
 }
 
 // ---- runtime helpers ----

@@ -41,7 +41,9 @@ namespace wc {
 template <class T>
 int threshold_to(const T* in, T* out, int64_t n, int J, int ttype, double t, int hardness,
                  int minl, int maxl, int copy_scaling, cudaStream_t s);
-int cv_sequential_sum(const double* terms, int64_t count, double* dev_out, cudaStream_t s);
+int cv_sequential_sum(const double* terms, int64_t count, double* dev_out, void* scratch,
+                      cudaStream_t s);
+size_t cv_sum_scratch_bytes(int64_t count);
 
 namespace {
 
@@ -152,10 +154,13 @@ int half_step(const Ctx<T>& c, const T* wcoef, HalfVec<T>& y, double t) {
 
 template <class T>
 int loss(const Ctx<T>& c, const HalfVec<T>& ye, const HalfVec<T>& yo, const double* xn,
-         double* terms, double* dsum, double* m) {
-  cv_terms_kernel<T><<<grid_for(c.lenh), kThreads, 0, c.s>>>(ye.x(), yo.x(), xn, c.lenh, terms);
+         double* terms, double* dsum, void* sum_scratch, double* m) {
+  {
+    LaunchTimer lt("cv_terms", c.s);
+    cv_terms_kernel<T><<<grid_for(c.lenh), kThreads, 0, c.s>>>(ye.x(), yo.x(), xn, c.lenh, terms);
+  }
   WC_TRY(after_launch("cv_terms_kernel"));
-  WC_TRY(cv_sequential_sum(terms, c.lenh, dsum, c.s));
+  WC_TRY(cv_sequential_sum(terms, c.lenh, dsum, sum_scratch, c.s));
   WC_CUDA(cudaMemcpyAsync(m, dsum, sizeof(double), cudaMemcpyDeviceToHost, c.s));
   WC_CUDA(cudaStreamSynchronize(c.s));
   return WC_OK;
@@ -237,9 +242,12 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
     WC_CUDA(cudaMemsetAsync(y[0].buf[0], 0,
                             (size_t)(reinterpret_cast<char*>(y[3].mod + hlen) -
                                      reinterpret_cast<char*>(y[0].buf[0])), s));
-    double* terms = static_cast<double*>(workspace(kSlotCvTerms, sizeof(double) * (size_t)(lenh + 64)));
-    if (!terms) return workspace_error();
+    const size_t tbytes = ((sizeof(double) * (size_t)(lenh + 64) + 255) / 256) * 256;
+    char* tbase = static_cast<char*>(workspace(kSlotCvTerms, tbytes + cv_sum_scratch_bytes(lenh)));
+    if (!tbase) return workspace_error();
+    double* terms = reinterpret_cast<double*>(tbase);
     double* dsum = terms + lenh + 32;
+    void* sscr = tbase + tbytes;
 
     split_even_odd<T><<<grid_for(lenh), kThreads, 0, s>>>(x, lenh, we, wo);
     WC_TRY(after_launch("split_even_odd"));
@@ -259,8 +267,8 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
     WC_TRY(half_step(c, wec, y[2], t2));
     WC_TRY(half_step(c, woc, y[3], t2));
     double m1, m2;
-    WC_TRY(loss(c, y[0], y[1], x, terms, dsum, &m1));
-    WC_TRY(loss(c, y[2], y[3], x, terms, dsum, &m2));
+    WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
+    WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
     while (fabs(t3 - t0) > tol * (t1 + t2)) {
       if (iters > 50) break;
       if (m1 != 0.0) min_margin = std::min(min_margin, fabs(m1 - m2) / fabs(m1));
@@ -269,13 +277,13 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
         m1 = m2;
         WC_TRY(half_step(c, wec, y[2], t2));
         WC_TRY(half_step(c, woc, y[3], t2));
-        WC_TRY(loss(c, y[2], y[3], x, terms, dsum, &m2));
+        WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
       } else {
         t3 = t2; t2 = t1; t1 = R * t1 + C * t0;
         m2 = m1;
         WC_TRY(half_step(c, wec, y[0], t1));
         WC_TRY(half_step(c, woc, y[1], t1));
-        WC_TRY(loss(c, y[0], y[1], x, terms, dsum, &m1));
+        WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
       }
       iters++;
     }
