@@ -194,6 +194,11 @@ typedef struct {
 WC_API int wc_profile_start(void);
 WC_API int wc_profile_stop(wc_kernel_time* out, int capacity, int* count);
 
+/* Reads and clears the current device's status word after synchronising:
+ * bit 0 set means a bounded device-side wait (bulk-copy barrier) gave up and
+ * the kernel that waited skipped its work.  0 when all is well. */
+WC_API int wc_device_status(unsigned int* status);
+
 /* Number of kernels this library launched in this process so far. */
 WC_API int64_t wc_kernel_launch_count(void);
 /* Frees the workspace, streams and events the library holds. */

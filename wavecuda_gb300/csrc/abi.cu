@@ -143,6 +143,17 @@ void* workspace(Slot slot, size_t bytes) {
   return p;
 }
 
+unsigned int* device_status_word() {
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    DeviceState& st = state();
+    if (st.slot[kSlotStatus]) return static_cast<unsigned int*>(st.slot[kSlotStatus]);
+  }
+  void* p = workspace(kSlotStatus, 256);
+  if (p) cudaMemset(p, 0, 256);
+  return static_cast<unsigned int*>(p);
+}
+
 int workspace_error() { return g_ws_err == WC_OK ? WC_ERR_NOMEM : g_ws_err; }
 
 int ensure_device() {
@@ -528,6 +539,19 @@ int wc_event_elapsed_ms(void* start, void* stop, float* ms) {
   return WC_OK;
 }
 int64_t wc_kernel_launch_count(void) { return g_launches.load(); }
+
+int wc_device_status(unsigned int* status) {
+  clear_error();
+  WC_TRY(ensure_device());
+  unsigned int* w = device_status_word();
+  if (!w) return workspace_error();
+  WC_CUDA(cudaDeviceSynchronize());
+  unsigned int h = 0;
+  WC_CUDA(cudaMemcpy(&h, w, sizeof(h), cudaMemcpyDeviceToHost));
+  WC_CUDA(cudaMemset(w, 0, sizeof(unsigned int)));
+  *status = h;
+  return WC_OK;
+}
 
 int wc_profile_start(void) {
   std::lock_guard<std::mutex> lk(g_prof_mu);

@@ -19,8 +19,10 @@
 // (s,d)[q-j], j < L/2, so the left halo is need_l = ceil(need_{l-1}/2) + L/2-1
 // coefficients at level l.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
+#include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
 
@@ -28,6 +30,14 @@ namespace wc {
 namespace {
 
 constexpr int kThreads = 256;
+
+// Element counts rounded up to a 16-byte multiple (bulk-copy granularity and
+// alignment of the shared-memory regions).
+template <class X>
+__host__ __device__ constexpr int64_t pad16(int64_t n) {
+  constexpr int64_t k = 16 / (int64_t)sizeof(X) > 0 ? 16 / (int64_t)sizeof(X) : 1;
+  return ((n + k - 1) / k) * k;
+}
 
 // Right halo of the forward pass at level l of G (in level-l values).
 __host__ __device__ constexpr int64_t fwd_halo(int L, int G, int l) {
@@ -42,36 +52,64 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
     d = haar_dif<P>(src[0], src[1]);
   } else {
     constexpr int L = filter_len(F);
-    s = P::mul(src[0], tap_h(F, 0));
-    d = P::mul(src[0], tap_g(F, 0));
+    typename P::Acc as = P::acc_init(src[0], tap_h(F, 0));
+    typename P::Acc ad = P::acc_init(src[0], tap_g(F, 0));
 #pragma unroll
     for (int j = 1; j < L; j++) {
-      s = P::madd(s, src[j], tap_h(F, j));
-      d = P::madd(d, src[j], tap_g(F, j));
+      as = P::acc_add(as, src[j], tap_h(F, j));
+      ad = P::acc_add(ad, src[j], tap_g(F, j));
     }
+    s = P::acc_fin(as);
+    d = P::acc_fin(ad);
   }
 }
 
 // Forward pass.  y[m] = in[m] (m < N, compact).  Writes the tile's
 // interleaved result to out[(t0+m)*S] and its level-G scaling values to
-// coarse[t0/2^G + k] (when coarse != nullptr).
+// coarse[t0/2^G + k] (when coarse != nullptr).  With `bulk` set, the tile and
+// its halo arrive by bulk copies (one or two: the halo of the last tile wraps
+// to the start) and, for S == 1, the result leaves by one bulk store.
 template <int F, class P>
 __global__ void __launch_bounds__(kThreads)
 dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
              typename P::T* __restrict__ out, int64_t S,
-             typename P::T* __restrict__ coarse, int write_coarse_slots) {
+             typename P::T* __restrict__ coarse, int write_coarse_slots, int bulk,
+             unsigned int* status) {
   using V = typename P::V;
+  using T = typename P::T;
   constexpr int L = filter_len(F);
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  const int64_t H0 = pad16<T>(fwd_halo(L, G, 0));
   V* A = reinterpret_cast<V*>(smem_raw);
-  const int64_t H0 = fwd_halo(L, G, 0);
-  V* B = A + (Tt + H0);
-  V* Z = B + (Tt / 2 + fwd_halo(L, G, 1));
+  V* B = A + pad16<V>(Tt + H0);
+  V* Z = B + pad16<V>(Tt / 2 + fwd_halo(L, G, 1));
   const int64_t t0 = (int64_t)blockIdx.x * Tt;
 
-  for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
-    A[m] = P::ld(in[wrap(t0 + m, N)]);
-  __syncthreads();
+  if (bulk) {
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&bar, (uint32_t)((Tt + H0) * sizeof(T)));
+      if (t0 + Tt + H0 <= N) {
+        bulk_g2s(A, in + t0, (uint32_t)((Tt + H0) * sizeof(T)), &bar);
+      } else {
+        bulk_g2s(A, in + t0, (uint32_t)(Tt * sizeof(T)), &bar);
+        if (H0 > 0) bulk_g2s(reinterpret_cast<T*>(A) + Tt, in, (uint32_t)(H0 * sizeof(T)), &bar);
+      }
+    }
+    const bool ok = mbar_wait(&bar, 0, status);
+    if (__syncthreads_or(!ok)) return;
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+        A[m] = P::ld(reinterpret_cast<const T*>(A)[m]);
+      __syncthreads();
+    }
+  } else {
+    for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+      A[m] = P::ld(in[wrap(t0 + m, N)]);
+    __syncthreads();
+  }
 
   V* src = A;
   V* dst = B;
@@ -94,6 +132,23 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
   }
   __syncthreads();
+  if (bulk && S == 1) {
+    T* Zt = reinterpret_cast<T*>(Z);
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+        const V v = Z[m];
+        Zt[m] = P::st(v);
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_s2g(out + t0, Zt, (uint32_t)(Tt * sizeof(T)));
+      bulk_commit();
+      bulk_wait_read();
+    }
+    return;
+  }
   const int64_t cmask = ((int64_t)1 << G) - 1;
   for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
     if (write_coarse_slots || (m & cmask) != 0) out[(t0 + m) * S] = P::st(Z[m]);
@@ -114,17 +169,41 @@ __global__ void __launch_bounds__(kThreads)
 dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
              const typename P::T* __restrict__ det, int64_t S, int64_t N, int G,
              int64_t Tt, typename P::T* __restrict__ outp, int64_t ostride,
-             InvGeom geo) {
+             InvGeom geo, int bulk, unsigned int* status) {
   using V = typename P::V;
+  using T = typename P::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
   const int64_t H = (int64_t)geo.need[G] << G;  // left halo of the staged array
   V* Z = reinterpret_cast<V*>(smem_raw);
-  V* SA = Z + (Tt + H);
-  V* SB = SA + (Tt + 2 * geo.off[0] + 16);
+  V* SA = Z + pad16<V>(Tt + H);
+  V* SB = SA + pad16<V>(Tt + 2 * geo.off[0] + 16);
   const int64_t t0 = (int64_t)blockIdx.x * Tt;
 
-  for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
-    Z[m] = P::ld(det[wrap(t0 - H + m, N) * S]);
+  if (bulk) {
+    // S == 1: the staged range [t0-H, t0+Tt) is contiguous except that the
+    // first tile's halo wraps to the end of the array.
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&bar, (uint32_t)((Tt + H) * sizeof(T)));
+      if (t0 >= H) {
+        bulk_g2s(Z, det + (t0 - H), (uint32_t)((Tt + H) * sizeof(T)), &bar);
+      } else {
+        bulk_g2s(Z, det + (N - H), (uint32_t)(H * sizeof(T)), &bar);
+        bulk_g2s(reinterpret_cast<T*>(Z) + H, det + t0, (uint32_t)(Tt * sizeof(T)), &bar);
+      }
+    }
+    const bool ok = mbar_wait(&bar, 0, status);
+    if (__syncthreads_or(!ok)) return;
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+        Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
+    }
+  } else {
+    for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+      Z[m] = P::ld(det[wrap(t0 - H + m, N) * S]);
+  }
   {
     const int64_t NG = N >> G, q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
     V* buf = (G & 1) ? SB : SA;  // level-G buffer; level 0 ends in SA
@@ -154,26 +233,47 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
         e = haar_sum<P>(sv[0], dv[0]);
         o = haar_dif<P>(sv[0], dv[0]);
       } else {
-        e = P::mul(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
-        o = P::mul(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
-        e = P::madd(e, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
-        o = P::madd(o, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+        typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+        typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+        ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+        ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
 #pragma unroll
         for (int j = HH - 2; j >= 0; j--) {
-          e = P::madd(e, sv[j], tap_h(F, 2 * j));
-          o = P::madd(o, sv[j], tap_h(F, 2 * j + 1));
-          e = P::madd(e, dv[j], tap_g(F, 2 * j));
-          o = P::madd(o, dv[j], tap_g(F, 2 * j + 1));
+          ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+          ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+          ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+          ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
         }
+        e = P::acc_fin(ae);
+        o = P::acc_fin(ao);
       }
       dst[2 * qr + geo.off[l - 1]] = e;
       dst[2 * qr + 1 + geo.off[l - 1]] = o;
     }
     __syncthreads();
   }
+  if (bulk && ostride == 1) {
+    T* St = reinterpret_cast<T*>(SA);
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+        const V v = SA[m];
+        St[m] = P::st(v);
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_s2g(outp + t0, St, (uint32_t)(Tt * sizeof(T)));
+      bulk_commit();
+      bulk_wait_read();
+    }
+    return;
+  }
   for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x)
     outp[(t0 + m) * ostride] = P::st(SA[m + geo.off[0]]);
 }
+
+bool aligned16_host(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 struct PassPlan {
   int64_t N, S, Tt;
@@ -184,8 +284,10 @@ constexpr size_t kSmemBudget = 100 * 1024;
 
 template <class P>
 size_t fwd_smem(int L, int G, int64_t Tt) {
-  return sizeof(typename P::V) * (size_t)(Tt + fwd_halo(L, G, 0) + Tt / 2 +
-                                          fwd_halo(L, G, 1) + Tt);
+  using V = typename P::V;
+  using T = typename P::T;
+  return sizeof(V) * (size_t)(pad16<V>(Tt + pad16<T>(fwd_halo(L, G, 0))) +
+                              pad16<V>(Tt / 2 + fwd_halo(L, G, 1)) + pad16<V>(Tt));
 }
 
 InvGeom inv_geom(int L, int G) {
@@ -201,7 +303,8 @@ template <class P>
 size_t inv_smem(int L, int G, int64_t Tt) {
   InvGeom g = inv_geom(L, G);
   int64_t H = (int64_t)g.need[G] << G;
-  return sizeof(typename P::V) * (size_t)((Tt + H) + 2 * (Tt + 2 * g.off[0] + 16));
+  using V = typename P::V;
+  return sizeof(V) * (size_t)(pad16<V>(Tt + H) + 2 * pad16<V>(Tt + 2 * g.off[0] + 16));
 }
 
 template <class P>
@@ -233,6 +336,8 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
   const T* in = static_cast<const T*>(vin);
   T* out = static_cast<T*>(vout);
   std::vector<PassPlan> plan = plan_passes<P>(n, J, F);
+  unsigned int* status = device_status_word();
+  if (!status) return workspace_error();
   const int np = (int)plan.size();
   T* scratch[2] = {nullptr, nullptr};
   if (np > 1) {
@@ -248,12 +353,18 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       const bool last = (p == np - 1);
       T* coarse = last ? nullptr : scratch[p & 1];
       size_t smem = fwd_smem<P>(L, pp.G, pp.Tt);
+      // Bulk staging needs 16-byte aligned tiles and a halo that wraps at
+      // most once.
+      const int64_t H0 = pad16<T>(fwd_halo(L, pp.G, 0));
+      const int bulk = aligned16_host(src) && aligned16_host(out) && H0 <= pp.N &&
+                       (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
       auto kern = dwt_fwd_pass<F, P>;
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       {
         LaunchTimer lt(p == 0 ? "dwt_fwd_pass0" : "dwt_fwd_pass", s);
         kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, pp.S,
-                                                             coarse, (last || pp.S == 1) ? 1 : 0);
+                                                             coarse, (last || pp.S == 1) ? 1 : 0,
+                                                             bulk, status);
       }
       WC_TRY(after_launch("dwt_fwd_pass"));
       src = coarse;
@@ -268,12 +379,16 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       T* dst = (p == 0) ? out : scratch[p & 1];
       InvGeom geo = inv_geom(L, pp.G);
       size_t smem = inv_smem<P>(L, pp.G, pp.Tt);
+      const int64_t H = (int64_t)geo.need[pp.G] << pp.G;
+      const int bulk = pp.S == 1 && H <= pp.N && aligned16_host(in) && aligned16_host(dst) &&
+                       (H * (int64_t)sizeof(T)) % 16 == 0 && (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
       auto kern = dwt_inv_pass<F, P>;
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       {
         LaunchTimer lt(p == 0 ? "dwt_inv_pass0" : "dwt_inv_pass", s);
         kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(coarse, cstride, in, pp.S, pp.N,
-                                                             pp.G, pp.Tt, dst, 1, geo);
+                                                             pp.G, pp.Tt, dst, 1, geo, bulk,
+                                                             status);
       }
       WC_TRY(after_launch("dwt_inv_pass"));
       coarse = dst;

@@ -38,15 +38,15 @@ modwt_fwd_level(const typename P::T* __restrict__ X, typename P::T* __restrict__
     } else {
       constexpr int L = filter_len(F);
       V v = P::ld(X[i]);
-      V d = P::mul(v, tap_g(F, 0)), s = P::mul(v, tap_h(F, 0));
+      typename P::Acc d = P::acc_init(v, tap_g(F, 0)), s = P::acc_init(v, tap_h(F, 0));
 #pragma unroll
       for (int k = 1; k < L; k++) {
         v = P::ld(X[wrap(i + (int64_t)k * skip, n)]);
-        d = P::madd(d, v, tap_g(F, k));
-        s = P::madd(s, v, tap_h(F, k));
+        d = P::acc_add(d, v, tap_g(F, k));
+        s = P::acc_add(s, v, tap_h(F, k));
       }
-      D[i] = P::st(d);
-      S[i] = P::st(s);
+      D[i] = P::st(P::acc_fin(d));
+      S[i] = P::st(P::acc_fin(s));
     }
   }
 }
@@ -66,17 +66,17 @@ modwt_inv_level(typename P::T* __restrict__ Xout, const typename P::T* __restric
       Xout[i] = P::st(P::mul(acc, kHInvR2));
     } else {
       constexpr int L = filter_len(F);
-      V acc;
+      typename P::Acc acc;
 #pragma unroll
       for (int t = 0; t < L; t++) {
         // even taps L-2, ..., 0 then odd taps L-1, ..., 1
         const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
         const int64_t j = wrap(i - (int64_t)k * skip, n);
-        if (t == 0) acc = P::mul(P::ld(S[j]), tap_h(F, k));
-        else acc = P::madd(acc, P::ld(S[j]), tap_h(F, k));
-        acc = P::madd(acc, P::ld(D[j]), tap_g(F, k));
+        if (t == 0) acc = P::acc_init(P::ld(S[j]), tap_h(F, k));
+        else acc = P::acc_add(acc, P::ld(S[j]), tap_h(F, k));
+        acc = P::acc_add(acc, P::ld(D[j]), tap_g(F, k));
       }
-      Xout[i] = P::st(P::half(acc));
+      Xout[i] = P::st(P::half(P::acc_fin(acc)));
     }
   }
 }

@@ -53,9 +53,20 @@ constexpr double kHInvR2 = 0.35355339059327376220;  // haarcoeffs.h:5
 // contraction), which is what makes its results bit-identical to the
 // reference's CPU code.
 
+// Dot products (a filter applied to L values) go through an accumulator:
+//   Acc a = acc_init(v0, c0);  a = acc_add(a, v_k, c_k) ...;  V r = acc_fin(a)
+// which for PExact is exactly mul, then add(acc, mul) in order -- the
+// reference's expression order -- and lets the double-float policy defer
+// its renormalisation to the end of the dot product.
 struct PExact {
   using T = double;
   using V = double;
+  using Acc = double;
+  static __device__ __forceinline__ Acc acc_init(V a, double c) { return __dmul_rn(a, c); }
+  static __device__ __forceinline__ Acc acc_add(Acc s, V a, double c) {
+    return __dadd_rn(s, __dmul_rn(a, c));
+  }
+  static __device__ __forceinline__ V acc_fin(Acc s) { return s; }
   static __device__ __forceinline__ V ld(T x) { return x; }
   static __device__ __forceinline__ T st(V v) { return v; }
   static __device__ __forceinline__ V mul(V a, double c) { return __dmul_rn(a, c); }
@@ -71,6 +82,12 @@ struct PExact {
 struct PF32 {
   using T = float;
   using V = float;
+  using Acc = float;
+  static __device__ __forceinline__ Acc acc_init(V a, double c) { return a * (float)c; }
+  static __device__ __forceinline__ Acc acc_add(Acc s, V a, double c) {
+    return __fmaf_rn(a, (float)c, s);
+  }
+  static __device__ __forceinline__ V acc_fin(Acc s) { return s; }
   static __device__ __forceinline__ V ld(T x) { return x; }
   static __device__ __forceinline__ T st(V v) { return v; }
   static __device__ __forceinline__ V mul(V a, double c) { return a * (float)c; }

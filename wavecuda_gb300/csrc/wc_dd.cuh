@@ -3,12 +3,25 @@
 // GB300's FP64 pipe is a small fraction of its FP32 rate, so WC_F64_FAST keeps
 // the data as FP64 in HBM but computes on the FP32 pipes with unevaluated
 // float pairs (hi + lo).  The building blocks are the error-free transforms
-// of Dekker (1971) and Knuth (TAOCP vol. 2): TwoSum, FastTwoSum and the
-// FMA-based TwoProd; products with a filter tap c use c split at compile time
-// into (ch, cl) = (fl32(c), fl32(c - ch)).  A value carries about 48
-// significant bits (relative error near 2^-47 per operation), and the
-// exponent range is that of FP32: the fast kernels are only used for inputs
-// whose magnitudes lie well inside it (see range checks at the ABI).
+// of Dekker (1971) and Knuth (TAOCP vol. 2, section 4.2.2): TwoSum,
+// FastTwoSum and the FMA-based TwoProduct.  Filter taps c are split at
+// compile time into (ch, cl) = (fl32(c), fl32(c - ch)).
+//
+// Dot products use the compensated scheme of Ogita, Rump and Oishi ("Dot2",
+// SIAM J. Sci. Comput. 26(6), 2005): the high parts of the products are
+// summed with TwoSum, every rounding error (product errors, cross terms
+// xh*cl + xl*ch, sum errors) goes into one float, and the pair is
+// renormalised once per output.  About 12 FP32 instructions per tap.
+//
+// Conversions never touch the FP64 pipe.  A double x = (-1)^s 2^e 1.f is
+// split by bit manipulation: hi keeps the top 23 fraction bits (exact,
+// truncated); the next 23 bits become lo through the implicit-bit trick
+// lo = float(s, e-23, f') - float(s, e-23, 0), an exact FP32 subtraction.
+// The split keeps 47 significant bits (relative error below 2^-46).  Values
+// whose exponent is outside [-100, 127] take the generic path through the
+// FP64 conversion instructions; magnitudes above the FP32 range are not
+// representable in this precision (use WC_F64_EXACT for them).
+// Back to FP64 by integer assembly as well (dd_to_double).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -20,48 +33,122 @@ struct dd {
   float hi, lo;
 };
 
-__device__ __forceinline__ dd two_sum(float a, float b) {
-  float s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-__device__ __forceinline__ dd fast_two_sum(float a, float b) {  // |a| >= |b|
-  float s = __fadd_rn(a, b);
-  float e = __fsub_rn(b, __fsub_rn(s, a));
-  return {s, e};
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
 }
 
-// Exact split of a double into hi = fl32(x) and lo = fl32(x - hi).
+// Generic conversions through the FP64 unit, kept out of line so that the
+// hot paths below never issue an FP64 instruction (an inlined fallback would
+// be predicated and executed for every element).
+static __device__ __noinline__ dd dd_from_double_slow(double x) {
+  if (x == 0.0) return {0.f, 0.f};
+  const float hi = __double2float_rn(x);
+  return {hi, __double2float_rn(x - (double)hi)};
+}
+static __device__ __noinline__ double dd_to_double_slow(float hi, float lo) {
+  return (double)hi + (double)lo;
+}
+
 __device__ __forceinline__ dd dd_from_double(double x) {
-  float hi = __double2float_rn(x);
-  float lo = __double2float_rn(x - (double)hi);
-  return {hi, lo};
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hw = (unsigned int)(b >> 32);
+  const int E = (int)((hw >> 20) & 0x7FF);  // biased FP64 exponent
+  // ef = E - 1023 + 127; lo's exponent ef - 23 must stay >= 1.
+  if (E < 1023 - 100 || E > 1023 + 127) return dd_from_double_slow(x);
+  const unsigned int sign = hw & 0x80000000u;
+  const unsigned int ef = (unsigned int)(E - 896);
+  const unsigned long long f = b & ((1ull << 52) - 1);
+  const float hi = __uint_as_float(sign | (ef << 23) | (unsigned int)(f >> 29));
+  const unsigned int rb = (unsigned int)((f >> 6) & 0x7FFFFF);  // next 23 bits
+  const float t = __uint_as_float(sign | ((ef - 23) << 23) | rb);
+  const float base = __uint_as_float(sign | ((ef - 23) << 23));
+  return {hi, __fsub_rn(t, base)};
 }
 
+// hi + lo as an FP64 value, assembled with integer operations: hi's 24-bit
+// significand is placed at the top of a 53-bit one, lo's significand is
+// shifted into place and added or subtracted, and one normalising shift
+// fixes a carry or borrow (|lo| <= ulp(hi) for every pair this library
+// builds).  lo's bits below the 53-bit window are truncated, an error below
+// one FP64 ulp.
 __device__ __forceinline__ double dd_to_double(dd v) {
-  return (double)v.hi + (double)v.lo;
+  const unsigned int hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const unsigned int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
+  if (eh == 0 || eh == 0xFF || el == 0xFF) return dd_to_double_slow(v.hi, v.lo);
+  unsigned long long A = (unsigned long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
+  if (el != 0) {
+    const unsigned long long ml = (lb & 0x7FFFFFu) | 0x800000u;
+    const int d = (int)eh - (int)el;
+    unsigned long long B;
+    if (d <= 29) B = ml << (29 - d);
+    else B = (d - 29 < 64) ? (ml >> (d - 29)) : 0ull;
+    A = ((hb ^ lb) & 0x80000000u) ? A - B : A + B;
+  }
+  int e = (int)eh + (1023 - 127);
+  if (A >> 53) {
+    A >>= 1;
+    e++;
+  } else if (!(A >> 52)) {
+    A <<= 1;
+    e--;
+  }
+  const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
+                                  ((unsigned long long)e << 52) | (A & ((1ull << 52) - 1));
+  return __longlong_as_double((long long)bits);
 }
+
+struct dd_acc {
+  float s, e;
+};
 
 struct PDD {
   using T = double;
   using V = dd;
+  using Acc = dd_acc;
   static __device__ __forceinline__ V ld(T x) { return dd_from_double(x); }
   static __device__ __forceinline__ T st(V v) { return dd_to_double(v); }
-  static __device__ __forceinline__ V mul(V a, double c) {
+
+  static __device__ __forceinline__ Acc acc_init(V a, double c) {
     const float ch = (float)c;
     const float cl = (float)(c - (double)ch);
-    float p = __fmul_rn(a.hi, ch);
+    const float p = __fmul_rn(a.hi, ch);
     float e = __fmaf_rn(a.hi, ch, -p);
     e = __fmaf_rn(a.hi, cl, e);
     e = __fmaf_rn(a.lo, ch, e);
-    return fast_two_sum(p, e);
+    return {p, e};
   }
+  static __device__ __forceinline__ Acc acc_add(Acc A, V a, double c) {
+    const float ch = (float)c;
+    const float cl = (float)(c - (double)ch);
+    const float p = __fmul_rn(a.hi, ch);
+    float pe = __fmaf_rn(a.hi, ch, -p);
+    pe = __fmaf_rn(a.hi, cl, pe);
+    pe = __fmaf_rn(a.lo, ch, pe);
+    float s, t;
+    two_sum(A.s, p, s, t);
+    return {s, __fadd_rn(A.e, __fadd_rn(pe, t))};
+  }
+  static __device__ __forceinline__ V acc_fin(Acc A) {
+    V r;
+    two_sum(A.s, A.e, r.hi, r.lo);
+    return r;
+  }
+
+  static __device__ __forceinline__ V mul(V a, double c) { return acc_fin(acc_init(a, c)); }
   static __device__ __forceinline__ V add(V a, V b) {
-    dd s = two_sum(a.hi, b.hi);
-    float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
-    return fast_two_sum(s.hi, e);
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    V r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
   }
   static __device__ __forceinline__ V sub(V a, V b) { return add(a, {-b.hi, -b.lo}); }
   static __device__ __forceinline__ V madd(V acc, V a, double c) { return add(acc, mul(a, c)); }

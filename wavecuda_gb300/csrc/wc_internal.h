@@ -63,6 +63,8 @@ enum Slot {
   kSlotCvTerms,      // cross-validation loss terms
   kSlotReduce,       // reductions (counts, sums)
   kSlotConvert,      // FP32 conversions at the boundary
+  kSlotStatus,       // device status word
+  kSlotBatch,        // batched smoothing (descriptors, results, CTA scratch)
   kNumSlots
 };
 
@@ -70,6 +72,10 @@ enum Slot {
 // device (nullptr plus an error on failure).
 void* workspace(Slot slot, size_t bytes);
 int workspace_error();  // WC_ERR_NOMEM / WC_ERR_CUDA of the last workspace() failure
+
+// Per-device status word that kernels OR error bits into (bit 0: a bounded
+// device-side wait gave up); zero-initialised when first created.
+unsigned int* device_status_word();
 
 // The library's own non-blocking stream on the current device.
 cudaStream_t lib_stream();
