@@ -398,6 +398,25 @@ def reference(args):
     print(json.dumps(out), flush=True)
 
 
+def profile_case(args):
+    """Runs one small single-kernel case twice (for ncu captures)."""
+    import wavecuda_gb300 as wc
+    n = 1 << args.log2n
+    x = np.random.default_rng(0).standard_normal(n)
+    L = wc.lib()
+    a, b = wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n * 2 * 4)
+    a.upload(x)
+    kind, filt, prec = args.profile_case.split(":")
+    filt, prec = int(filt), int(prec)
+    for _ in range(2):
+        if kind == "dwt":
+            wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, min(16, args.log2n - 2), filt, prec, None))
+        else:
+            wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 1, 4, filt, prec, None))
+        wc.check(L.wc_stream_synchronize(None))
+    print("ok", args.profile_case)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,8 +432,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-log2n", type=int, default=24)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--profile-case", default=None,
+                    help="kind:filter:precision, e.g. dwt:2:1 -- one small case for ncu")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.impl == "reference":
         reference(args)
     else:
         ours(args)

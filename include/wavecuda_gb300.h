@@ -140,6 +140,53 @@ WC_API int wc_smooth(double* x, int64_t len, int nlevels, int ttype, int filter,
               int threshtype, double* thresh, int hardness, int minlevel,
               int maxlevel, double tol, int precision, wc_smooth_info* info);
 
+/* ---- batched smoothing: many signals of uneven length, filter, transform
+ * and level count smoothed by one persistent launch.  The shape of the
+ * reference's (placeholder) list API RgpuTransformList, rfunctions.cu:139-154,
+ * in flat .C-friendly form: signals live back to back in one FP64 array and
+ * are described by wc_signal records. */
+typedef struct {
+  int64_t offset;   /* first element of the signal in the data array */
+  int64_t len;      /* power of two */
+  int nlevels;      /* 0 = maximum */
+  int ttype;        /* DWT 0 / MODWT 1 */
+  int filter;       /* 1..4 */
+  int threshtype;   /* MANUAL 0 / UNIV 1 / CV 2 */
+  int hardness;     /* HARD 0 / SOFT 1 */
+  int minlevel, maxlevel;
+  double thresh;    /* threshold for MANUAL */
+  double tol;       /* CV tolerance */
+} wc_signal;
+
+typedef struct {
+  double thresh;        /* threshold applied */
+  double thresh_univ;   /* universal threshold (CV bracket) */
+  double min_margin;    /* smallest |m1-m2|/m1 the CV search compared */
+  int iterations;       /* CV golden-section iterations */
+  int status;           /* WC_OK */
+  int64_t kept, zeroed; /* detail counts in [minlevel, maxlevel] */
+} wc_signal_result;
+
+typedef struct wc_batch_plan_s* wc_batch_plan;
+
+/* Validates the signals, orders the work queue largest-first, sizes the
+ * per-CTA scratch and allocates the plan's device buffers. */
+WC_API int wc_batch_plan_create(const wc_signal* signals, int nsig, int precision,
+                                wc_batch_plan* plan);
+WC_API int wc_batch_plan_destroy(wc_batch_plan plan);
+WC_API int wc_batch_plan_info(wc_batch_plan plan, int* grid, size_t* scratch_bytes);
+/* Times a few grid sizes on a scratch copy of data (device) and keeps the
+ * fastest; data is not modified. */
+WC_API int wc_batch_autotune(wc_batch_plan plan, const double* data, float* best_ms);
+/* Smooths every signal of data (device, FP64) in place: one CUDA-graph launch
+ * of the queue reset and the persistent kernel, asynchronous on stream. */
+WC_API int wc_batch_run_device(wc_batch_plan plan, double* data, void* stream);
+/* Copies the per-signal results to the host (synchronises stream). */
+WC_API int wc_batch_results(wc_batch_plan plan, wc_signal_result* results, void* stream);
+/* Host-buffer convenience: plan, copy in, run, copy out, results. */
+WC_API int wc_smooth_batch(double* data, int64_t total, const wc_signal* signals, int nsig,
+                           int precision, wc_signal_result* results);
+
 /* ---- device-pointer API: inputs and outputs already in HBM.  stream is a
  * cudaStream_t (NULL = the library's own stream).  Calls are asynchronous
  * with respect to the host unless stated; scratch comes from the library's

@@ -51,6 +51,20 @@ class SmoothInfo(C.Structure):
                 ("kept", C.c_int64), ("zeroed", C.c_int64), ("min_margin", C.c_double)]
 
 
+class Signal(C.Structure):
+    """wc_signal: one signal of a batch."""
+    _fields_ = [("offset", C.c_int64), ("len", C.c_int64), ("nlevels", C.c_int),
+                ("ttype", C.c_int), ("filter", C.c_int), ("threshtype", C.c_int),
+                ("hardness", C.c_int), ("minlevel", C.c_int), ("maxlevel", C.c_int),
+                ("thresh", C.c_double), ("tol", C.c_double)]
+
+
+class SignalResult(C.Structure):
+    _fields_ = [("thresh", C.c_double), ("thresh_univ", C.c_double),
+                ("min_margin", C.c_double), ("iterations", C.c_int), ("status", C.c_int),
+                ("kept", C.c_int64), ("zeroed", C.c_int64)]
+
+
 _lib: Optional[C.CDLL] = None
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -85,6 +99,15 @@ def lib() -> C.CDLL:
     L.wc_modwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
     L.wc_median_mad_device.argtypes = [_vp, C.c_int64, _dp, _dp, _vp]
     L.wc_sequential_sum_device.argtypes = [_vp, C.c_int64, _dp, _vp]
+    L.wc_batch_plan_create.argtypes = [C.POINTER(Signal), C.c_int, C.c_int, C.POINTER(_vp)]
+    L.wc_batch_plan_destroy.argtypes = [_vp]
+    L.wc_batch_plan_info.argtypes = [_vp, _ip, C.POINTER(C.c_size_t)]
+    L.wc_batch_autotune.argtypes = [_vp, _vp, C.POINTER(C.c_float)]
+    L.wc_batch_run_device.argtypes = [_vp, _vp, _vp]
+    L.wc_batch_results.argtypes = [_vp, C.POINTER(SignalResult), _vp]
+    L.wc_smooth_batch.argtypes = [_dp, C.c_int64, C.POINTER(Signal), C.c_int, C.c_int,
+                                  C.POINTER(SignalResult)]
+    L.wc_device_status.argtypes = [C.POINTER(C.c_uint)]
     L.wc_device_count.argtypes = [_ip]
     L.wc_malloc_device.argtypes = [C.POINTER(_vp), C.c_size_t]
     L.wc_free_device.argtypes = [_vp]
@@ -424,6 +447,22 @@ def sequential_sum(v) -> float:
     check(lib().wc_sequential_sum_device(buf.ptr, v.size, C.byref(out), None))
     buf.free()
     return out.value
+
+
+def smooth_batch(data, signals, precision=F64_EXACT):
+    """wc_smooth_batch: smooths every signal of the flat array `data` (host)
+    in one persistent launch; returns (smoothed copy, list of SignalResult)."""
+    y = np.array(data, dtype=np.float64, copy=True)
+    arr = (Signal * len(signals))(*signals)
+    res = (SignalResult * len(signals))()
+    check(lib().wc_smooth_batch(_dptr(y), y.size, arr, len(signals), precision, res))
+    return y, list(res)
+
+
+def device_status() -> int:
+    v = C.c_uint(0)
+    check(lib().wc_device_status(C.byref(v)))
+    return v.value
 
 
 def device_count() -> int:

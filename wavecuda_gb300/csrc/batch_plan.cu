@@ -1,0 +1,283 @@
+// Host side of batched smoothing: validation, per-signal constants, the
+// largest-work-first queue order, per-CTA scratch sizing, the grid size
+// (autotuned on request), and a CUDA graph that replays the queue reset and
+// the persistent launch.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "wc_batch.h"
+#include "wc_common.cuh"
+
+struct wc_batch_plan_s {
+  int nsig = 0;
+  int prec = 0;
+  int grid = 0;
+  size_t scratch_per_cta = 0;
+  int64_t total = 0;  // elements spanned by the batch (max off + n)
+  wc::BatchDesc* d_desc = nullptr;
+  wc::BatchResult* d_res = nullptr;
+  int* d_order = nullptr;
+  int* d_counter = nullptr;
+  char* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // graph cache
+  cudaGraphExec_t exec = nullptr;
+  double* graph_data = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int graph_grid = 0;
+};
+
+namespace wc {
+namespace {
+
+// Work estimate used for ordering: transform size times the CV search depth.
+double work_of(const BatchDesc& d) {
+  const double per = d.ttype == 1 ? (double)d.J : 2.0;
+  return (double)d.n * per * (d.threshtype == 2 ? 40.0 : 1.0);
+}
+
+void free_plan(wc_batch_plan_s* p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  cudaFree(p->d_desc);
+  cudaFree(p->d_res);
+  cudaFree(p->d_order);
+  cudaFree(p->d_counter);
+  cudaFree(p->d_scratch);
+  delete p;
+}
+
+int launch_direct(wc_batch_plan_s* p, double* data, int grid, cudaStream_t s) {
+  WC_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(int), s));
+  BatchArgs a{p->d_desc, p->d_res, p->d_order, p->d_counter, p->nsig, data, p->d_scratch,
+              p->scratch_per_cta};
+  LaunchTimer lt("smooth_batch", s);
+  return batch_launch(a, p->prec, grid, s);
+}
+
+}  // namespace
+}  // namespace wc
+
+using namespace wc;
+
+extern "C" {
+
+int wc_batch_plan_create(const wc_signal* sigs, int nsig, int precision, wc_batch_plan* out) {
+  clear_error();
+  if (!sigs || nsig <= 0 || !out) return fail(WC_ERR_ARG, "bad batch arguments");
+  if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
+  WC_TRY(ensure_device());
+  std::vector<BatchDesc> desc(nsig);
+  int64_t total = 0;
+  size_t per_cta = 0;
+  for (int i = 0; i < nsig; i++) {
+    const wc_signal& s = sigs[i];
+    if (s.filter < 1 || s.filter > 4) return fail(WC_ERR_ARG, "signal %d: unrecognised filter", i);
+    if (s.ttype != 0 && s.ttype != 1) return fail(WC_ERR_ARG, "signal %d: transform type", i);
+    if (s.threshtype < 0 || s.threshtype > 2) return fail(WC_ERR_ARG, "signal %d: threshold type", i);
+    if (s.offset < 0) return fail(WC_ERR_ARG, "signal %d: negative offset", i);
+    const int L = filter_len(s.filter);
+    const int J = check_levels(s.len, s.nlevels, L);
+    if (J == 0) return fail(WC_ERR_LEVELS, "signal %d: nlevels %d invalid for length %lld", i,
+                            s.nlevels, (long long)s.len);
+    if (s.threshtype == 2 && !(s.tol > 0)) return fail(WC_ERR_ARG, "signal %d: tolerance", i);
+    BatchDesc& d = desc[i];
+    d.off = s.offset;
+    d.n = s.len;
+    d.J = J;
+    d.ttype = s.ttype;
+    d.F = s.filter;
+    d.threshtype = s.threshtype;
+    d.hardness = s.hardness;
+    d.minl = s.minlevel;
+    d.maxl = s.maxlevel;
+    d.pad = 0;
+    d.thresh = s.thresh;
+    d.tol = s.tol;
+    // thresh.cpp:180,198,326 evaluated with the host libm, as the reference does
+    d.sq_n = sqrt(2. * log((double)s.len));
+    d.sq_nm1 = sqrt(2. * log((double)(s.len - 1)));
+    d.rescale = sqrt(1. - log(2.) / log((double)s.len));
+    total = std::max(total, s.offset + s.len);
+    per_cta = std::max(per_cta, batch_scratch_bytes(d, precision));
+  }
+  std::vector<int> order(nsig);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return work_of(desc[a]) > work_of(desc[b]); });
+
+  auto* p = new wc_batch_plan_s;
+  p->nsig = nsig;
+  p->prec = precision;
+  p->total = total;
+  p->scratch_per_cta = ((per_cta + 255) / 256) * 256;
+  // Grid: every resident CTA, limited so that the CTA scratch takes at most
+  // half of the free device memory.
+  size_t freeb = 0, totb = 0;
+  cudaMemGetInfo(&freeb, &totb);
+  int grid = batch_max_ctas(precision);
+  const size_t cap = (freeb / 2) / std::max<size_t>(p->scratch_per_cta, 1);
+  grid = (int)std::min<size_t>((size_t)grid, std::max<size_t>(cap, 1));
+  grid = std::min(grid, nsig);
+  p->grid = grid;
+  p->scratch_bytes = p->scratch_per_cta * (size_t)grid;
+  cudaError_t e = cudaSuccess;
+  if ((e = cudaMalloc(&p->d_desc, sizeof(BatchDesc) * nsig)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_res, sizeof(BatchResult) * nsig)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_order, sizeof(int) * nsig)) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_counter, sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_scratch, p->scratch_bytes)) != cudaSuccess) {
+    cudaGetLastError();
+    free_plan(p);
+    return fail(WC_ERR_NOMEM, "batch plan allocation failed: %s", cudaGetErrorString(e));
+  }
+  cudaMemcpy(p->d_desc, desc.data(), sizeof(BatchDesc) * nsig, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_order, order.data(), sizeof(int) * nsig, cudaMemcpyHostToDevice);
+  cudaMemset(p->d_res, 0, sizeof(BatchResult) * nsig);
+  *out = p;
+  return WC_OK;
+}
+
+int wc_batch_plan_destroy(wc_batch_plan plan) {
+  free_plan(plan);
+  return WC_OK;
+}
+
+int wc_batch_plan_info(wc_batch_plan plan, int* grid, size_t* scratch_bytes) {
+  if (!plan) return fail(WC_ERR_ARG, "null plan");
+  if (grid) *grid = plan->grid;
+  if (scratch_bytes) *scratch_bytes = plan->scratch_bytes;
+  return WC_OK;
+}
+
+int wc_batch_run_device(wc_batch_plan plan, double* data, void* stream) {
+  clear_error();
+  if (!plan || !data) return fail(WC_ERR_ARG, "null plan or data");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lib_stream();
+  if (!plan->exec || plan->graph_data != data || plan->graph_stream != s ||
+      plan->graph_grid != plan->grid) {
+    if (plan->exec) {
+      cudaGraphExecDestroy(plan->exec);
+      plan->exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    cudaStream_t cap = nullptr;
+    WC_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    WC_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int r = launch_direct(plan, data, plan->grid, cap);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (r != WC_OK) return r;
+    if (e != cudaSuccess) return fail(WC_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&plan->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(WC_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    plan->graph_data = data;
+    plan->graph_stream = s;
+    plan->graph_grid = plan->grid;
+  }
+  {
+    LaunchTimer lt("smooth_batch_graph", s);
+    WC_CUDA(cudaGraphLaunch(plan->exec, s));
+  }
+  count_launches(1);
+  return WC_OK;
+}
+
+int wc_batch_results(wc_batch_plan plan, wc_signal_result* out, void* stream) {
+  clear_error();
+  if (!plan || !out) return fail(WC_ERR_ARG, "null plan or output");
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : lib_stream();
+  std::vector<BatchResult> r(plan->nsig);
+  WC_CUDA(cudaMemcpyAsync(r.data(), plan->d_res, sizeof(BatchResult) * plan->nsig,
+                          cudaMemcpyDeviceToHost, s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < plan->nsig; i++) {
+    out[i].thresh = r[i].thresh;
+    out[i].thresh_univ = r[i].thresh_univ;
+    out[i].min_margin = r[i].min_margin;
+    out[i].iterations = r[i].iterations;
+    out[i].status = r[i].status;
+    out[i].kept = r[i].kept;
+    out[i].zeroed = r[i].zeroed;
+  }
+  return WC_OK;
+}
+
+// Times the batch at a few grid sizes on a scratch copy of the data and keeps
+// the fastest for the plan.  The data are not modified.
+int wc_batch_autotune(wc_batch_plan plan, const double* data, float* best_ms) {
+  clear_error();
+  if (!plan || !data) return fail(WC_ERR_ARG, "null plan or data");
+  cudaStream_t s = lib_stream();
+  double* copy = nullptr;
+  const size_t bytes = sizeof(double) * (size_t)plan->total;
+  WC_CUDA(cudaMalloc(&copy, bytes));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  std::vector<int> cand = {plan->grid};
+  for (int g : {sms / 2, sms, 2 * sms}) {
+    if (g >= 1 && g < plan->grid) cand.push_back(g);
+  }
+  std::sort(cand.begin(), cand.end());
+  cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int best_g = plan->grid;
+  int rc = WC_OK;
+  for (int g : cand) {
+    cudaMemcpyAsync(copy, data, bytes, cudaMemcpyDeviceToDevice, s);
+    cudaEventRecord(a, s);
+    rc = launch_direct(plan, copy, g, s);
+    cudaEventRecord(b, s);
+    if (rc != WC_OK) break;
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) {
+      best = ms;
+      best_g = g;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(copy);
+  if (rc != WC_OK) return rc;
+  plan->grid = best_g;
+  if (best_ms) *best_ms = best;
+  return WC_OK;
+}
+
+int wc_smooth_batch(double* data, int64_t total, const wc_signal* sigs, int nsig, int precision,
+                    wc_signal_result* results) {
+  clear_error();
+  if (!data || !sigs || !results || total <= 0) return fail(WC_ERR_ARG, "bad batch arguments");
+  for (int i = 0; i < nsig; i++)
+    if (sigs[i].offset + sigs[i].len > total)
+      return fail(WC_ERR_ARG, "signal %d extends past the data (%lld elements)", i, (long long)total);
+  wc_batch_plan plan = nullptr;
+  WC_TRY(wc_batch_plan_create(sigs, nsig, precision, &plan));
+  cudaStream_t s = lib_stream();
+  double* d = static_cast<double*>(workspace(kSlotBatch, sizeof(double) * (size_t)total));
+  int rc = d ? WC_OK : workspace_error();
+  if (rc == WC_OK && cudaMemcpyAsync(d, data, sizeof(double) * (size_t)total,
+                                     cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = fail(WC_ERR_CUDA, "copy to device failed");
+  if (rc == WC_OK) rc = wc_batch_run_device(plan, d, s);
+  if (rc == WC_OK && cudaMemcpyAsync(data, d, sizeof(double) * (size_t)total,
+                                     cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    rc = fail(WC_ERR_CUDA, "copy to host failed");
+  if (rc == WC_OK) rc = wc_batch_results(plan, results, s);
+  wc_batch_plan_destroy(plan);
+  return rc;
+}
+
+}  // extern "C"
