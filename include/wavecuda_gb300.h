@@ -198,6 +198,25 @@ WC_API int wc_smooth_batch(double* data, int64_t total, const wc_signal* signals
 WC_API int wc_dwt_device(const void* in, void* out, int64_t len, int sense,
                   int nlevels, int filter, int precision, void* stream);
 
+/* Allocation-free DWT.  No counterpart in the reference: an addition for
+ * callers that cannot let this library call cudaMalloc -- a host framework
+ * that has reserved nearly all device memory for its own pool, or a
+ * latency-critical loop that must not hit the synchronisation cudaFree
+ * brings when a workspace grows.  Same arguments and results as
+ * wc_dwt_device, but the scratch (coarse coefficients between passes and the
+ * status word) lives in one fixed 1 MiB + 256 B device array compiled into
+ * the library, which every GPU that loads it holds until the process exits.
+ * Limit: len <= 2^22 samples (longer lengths are rejected with WC_ERR_ARG).
+ * The first call on a device looks up the array's device address for that
+ * device; make it before any stream capture.  All calls share the array and
+ * it keeps the last call's contents, so calls that overlap on the GPU race.
+ * stream NULL means the legacy default stream (other wc_* calls given NULL
+ * use the library's non-blocking stream, which is not ordered with it, so
+ * pass the same explicit stream when mixing them).  Calls no cudaMalloc or
+ * cudaFree. */
+WC_API int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int sense,
+                                 int nlevels, int filter, int precision, void* stream);
+
 /* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
  * BWD reads only s_J and d_1..d_J. */
 WC_API int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlevels,

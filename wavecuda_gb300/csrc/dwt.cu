@@ -422,3 +422,159 @@ int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
 }
 
 }  // namespace wc
+
+// ---------------------------------------------------------------------------
+// Allocation-free DWT entry point (wc_dwt_device_noalloc).
+//
+// Some callers cannot let this library call cudaMalloc: a host framework that
+// has already reserved nearly all of HBM for its own memory pool (a
+// cudaMalloc from here would fail, or fragment that pool), or a latency-
+// critical loop that must not hit the device-wide synchronisation cudaFree
+// performs when the workspace grows.  For them the DWT's only scratch -- the
+// compact coarse coefficients handed from one pass to the next -- and the
+// device status word live in one file-scope device array of fixed size,
+// loaded with the library and held by every GPU that loads it until the
+// process exits.  Host code must not use the array's name as a device
+// address (it is a host-side stand-in); the device address comes from
+// cudaGetSymbolAddress, looked up once per device by the first call made
+// with that device current.  Make that first call before any stream capture.
+// All calls share the array and it keeps the last call's contents: calls
+// whose work overlaps on the GPU (different streams, or threads) race on it.
+#include <mutex>
+
+namespace wc {
+namespace {
+
+// Longest signal the allocation-free entry point accepts, and its scratch.
+constexpr int64_t kNoAllocMaxLen = (int64_t)1 << 22;
+constexpr size_t kNoAllocStatusBytes = 256;
+constexpr size_t kNoAllocCoarseBytes = (size_t)1 << 19;  // per coarse buffer
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[kNoAllocStatusBytes + 2 * kNoAllocCoarseBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_base[256] = {};
+
+// Device address of g_noalloc_scratch on the current device.
+int noalloc_base(unsigned char** base) {
+  int dev = 0;
+  WC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(WC_ERR_ARG, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return fail(WC_ERR_CUDA, "cudaGetSymbolAddress of the static DWT scratch failed: %s",
+                  cudaGetErrorString(e));
+    }
+    g_noalloc_base[dev] = p;
+  }
+  *base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+  return WC_OK;
+}
+
+// The DWT of run_dwt with its scratch taken from the static array.
+template <int F, class P>
+int run_dwt_noalloc(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream_t s,
+                    unsigned char* base) {
+  using T = typename P::T;
+  const int L = filter_len(F);
+  const T* in = static_cast<const T*>(vin);
+  T* out = static_cast<T*>(vout);
+  std::vector<PassPlan> plan = plan_passes<P>(n, J, F);
+  const int np = (int)plan.size();
+  unsigned int* status = reinterpret_cast<unsigned int*>(base);
+  T* scratch[2] = {reinterpret_cast<T*>(base + kNoAllocStatusBytes),
+                   reinterpret_cast<T*>(base + kNoAllocStatusBytes + kNoAllocCoarseBytes)};
+  if (np > 1 && sizeof(T) * (size_t)(plan[0].N >> plan[0].G) > kNoAllocCoarseBytes)
+    return fail(WC_ERR_ARG, "allocation-free DWT: coarse scratch of %zu bytes exceeds %zu",
+                sizeof(T) * (size_t)(plan[0].N >> plan[0].G), kNoAllocCoarseBytes);
+  // The status word must start at zero for this call.
+  WC_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned int), s));
+  if (sense == 1) {
+    const T* src = in;
+    for (int p = 0; p < np; p++) {
+      const PassPlan& pp = plan[p];
+      const bool last = (p == np - 1);
+      T* coarse = last ? nullptr : scratch[p & 1];
+      const size_t smem = fwd_smem<P>(L, pp.G, pp.Tt);
+      const int64_t H0 = pad16<T>(fwd_halo(L, pp.G, 0));
+      const int bulk = aligned16_host(src) && aligned16_host(out) && H0 <= pp.N &&
+                       (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
+      auto kern = dwt_fwd_pass<F, P>;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, pp.S,
+                                                           coarse, (last || pp.S == 1) ? 1 : 0,
+                                                           bulk, status);
+      WC_TRY(after_launch("dwt_fwd_pass"));
+      src = coarse;
+    }
+  } else {
+    const T* coarse = in;
+    int64_t cstride = plan[np - 1].S << plan[np - 1].G;
+    for (int p = np - 1; p >= 0; p--) {
+      const PassPlan& pp = plan[p];
+      T* dst = (p == 0) ? out : scratch[p & 1];
+      InvGeom geo = inv_geom(L, pp.G);
+      const size_t smem = inv_smem<P>(L, pp.G, pp.Tt);
+      const int64_t H = (int64_t)geo.need[pp.G] << pp.G;
+      const int bulk = pp.S == 1 && H <= pp.N && aligned16_host(in) && aligned16_host(dst) &&
+                       (H * (int64_t)sizeof(T)) % 16 == 0 &&
+                       (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
+      auto kern = dwt_inv_pass<F, P>;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(coarse, cstride, in, pp.S, pp.N,
+                                                           pp.G, pp.Tt, dst, 1, geo, bulk, status);
+      WC_TRY(after_launch("dwt_inv_pass"));
+      coarse = dst;
+      cstride = 1;
+    }
+  }
+  return WC_OK;
+}
+
+template <class P>
+int dispatch_noalloc(const void* in, void* out, int64_t n, int sense, int J, int F,
+                     cudaStream_t s, unsigned char* base) {
+  switch (F) {
+    case 1: return run_dwt_noalloc<1, P>(in, out, n, sense, J, s, base);
+    case 2: return run_dwt_noalloc<2, P>(in, out, n, sense, J, s, base);
+    case 3: return run_dwt_noalloc<3, P>(in, out, n, sense, J, s, base);
+    case 4: return run_dwt_noalloc<4, P>(in, out, n, sense, J, s, base);
+  }
+  return fail(WC_ERR_ARG, "unrecognised filter %d", F);
+}
+
+}  // namespace
+}  // namespace wc
+
+extern "C" int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int sense,
+                                     int nlevels, int filter, int precision, void* stream) {
+  using namespace wc;
+  clear_error();
+  WC_TRY(ensure_device());
+  if (filter < 1 || filter > 4) return fail(WC_ERR_ARG, "unrecognised filter %d", filter);
+  if (sense != 0 && sense != 1) return fail(WC_ERR_ARG, "sense must be 1 (FWD) or 0 (BWD)");
+  if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
+  if (len <= 0 || (len & (len - 1)) != 0)
+    return fail(WC_ERR_ARG, "length %lld is not a power of 2", (long long)len);
+  if (len > kNoAllocMaxLen)
+    return fail(WC_ERR_ARG,
+                "length %lld exceeds the allocation-free DWT's maximum of %lld samples "
+                "(use wc_dwt_device for longer signals)",
+                (long long)len, (long long)kNoAllocMaxLen);
+  const int J = check_levels(len, nlevels, filter_len(filter));
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
+  if (!in || !out || in == out) return fail(WC_ERR_ARG, "in and out must be distinct device buffers");
+  unsigned char* base = nullptr;
+  WC_TRY(noalloc_base(&base));
+  // No library stream is created here: NULL means the legacy default stream.
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (precision) {
+    case WC_F64_EXACT: return dispatch_noalloc<PExact>(in, out, len, sense, J, filter, s, base);
+    case WC_F64_FAST: return dispatch_noalloc<PDD>(in, out, len, sense, J, filter, s, base);
+    default: return dispatch_noalloc<PF32>(in, out, len, sense, J, filter, s, base);
+  }
+}
