@@ -255,6 +255,17 @@ def ours(args):
     x = signals.roofline_input(n, seed=1 + dist.rank)
     bufs[0].upload(x)
 
+    # Autotune the DWT first-pass tiling (setup, not timed).
+    tiling = {}
+    if not args.no_tune:
+        combos = {(filt, prec)}
+        if not args.no_sweep:
+            combos |= {(f, p) for f in (1, 2, 3, 4) for p in (0, 1, 2)}
+        for f, p in sorted(combos):
+            (tile, g0, th, pipe), tms = wc.tune_dwt(f, p, 24)
+            tiling[f"{FILTERS[f]}/{PREC[p]}"] = {"tile": tile, "g0": g0, "threads": th,
+                                                  "pipelined": pipe, "ms_2e24": round(tms, 4)}
+
     clocks = ClockSampler()
     clocks.start()
     ms, launches, prof = time_gpu(wc, bufs, n, filt, 0, J, prec, stream, args.steps, args.warmup,
@@ -357,6 +368,8 @@ def ours(args):
                     if p == 2:
                         xf.free()
         out["sweep"] = sweep
+    if tiling:
+        out["tiling"] = tiling
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -428,6 +441,7 @@ def main():
     ap.add_argument("--levels", type=int, default=16)
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-log2n", type=int, default=24)

@@ -217,6 +217,17 @@ WC_API int wc_dwt_device(const void* in, void* out, int64_t len, int sense,
 WC_API int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int sense,
                                  int nlevels, int filter, int precision, void* stream);
 
+/* First-pass tiling of the DWT per (filter, precision): tile (power of two,
+ * 256..16384 values per CTA), g0 (levels fused in the first pass), threads
+ * (256 or 512 per CTA) and pipelined (1: persistent CTAs with double-buffered
+ * bulk copies).  wc_tune_dwt times every candidate on a 2^log2n-sample signal
+ * (forward + inverse) and keeps the fastest; the setting is per process. */
+WC_API int wc_set_dwt_tiling(int filter, int precision, int tile, int g0, int threads,
+                             int pipelined);
+WC_API int wc_get_dwt_tiling(int filter, int precision, int* tile, int* g0, int* threads,
+                             int* pipelined);
+WC_API int wc_tune_dwt(int filter, int precision, int log2n, float* best_ms);
+
 /* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
  * BWD reads only s_J and d_1..d_J. */
 WC_API int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlevels,

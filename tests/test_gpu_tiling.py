@@ -1,0 +1,66 @@
+"""Every first-pass tiling of the DWT (tile size, fused levels, block size,
+pipelined persistent kernels or not) gives the oracle's result: bit-identical
+in WC_F64_EXACT, within the usual tolerances otherwise."""
+import numpy as np
+import pytest
+
+import pyoracle as P
+from wavecuda_gb300 import signals
+
+pytestmark = pytest.mark.gpu
+
+GMAX = {1: 12, 2: 8, 3: 7, 4: 6}
+
+
+def candidates(filt, prec):
+    tiles = (4096, 8192) if prec == 2 else (2048, 4096)
+    for tile in tiles:
+        for g in (GMAX[filt] - 1, GMAX[filt], 3):
+            if (1 << g) > tile:
+                continue
+            for th in (256, 512):
+                for pipe in (1, 0):
+                    yield tile, g, th, pipe
+
+
+@pytest.mark.parametrize("filt", [1, 2, 3, 4])
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_tilings_match_oracle(gpu, oracle, filt, prec):
+    keep = gpu.get_dwt_tiling(filt, prec)
+    n = 1 << 17
+    x = signals.roofline_input(n, seed=filt + 10 * prec)
+    J = min(16, oracle.levels(n, 0, filt))
+    w_ref = oracle.dwt(x, J, filt)
+    tol = {0: 0.0, 1: 1e-12, 2: 2e-5}[prec]
+    try:
+        for c in candidates(filt, prec):
+            gpu.set_dwt_tiling(filt, prec, *c)
+            w = gpu.transform(x, J, gpu.DWT, filt, gpu.FWD, prec)
+            err = np.max(np.abs(w - w_ref)) / np.max(np.abs(w_ref))
+            assert err <= tol, (c, err)
+            r = gpu.transform(w_ref, J, gpu.DWT, filt, gpu.BWD, prec)
+            if prec == 0:
+                assert np.array_equal(r, oracle.dwt(w_ref, J, filt, P.BWD)), c
+            else:
+                assert np.max(np.abs(r - x)) / np.max(np.abs(x)) <= 4 * tol, c
+        assert gpu.device_status() == 0
+    finally:
+        gpu.set_dwt_tiling(filt, prec, *keep)
+
+
+def test_tiling_rejects_bad_values(gpu):
+    with pytest.raises(gpu.WaveCudaError):
+        gpu.set_dwt_tiling(2, 0, 3000, 8, 256, 1)
+    with pytest.raises(gpu.WaveCudaError):
+        gpu.set_dwt_tiling(2, 0, 4096, 13, 256, 1)
+    with pytest.raises(gpu.WaveCudaError):
+        gpu.set_dwt_tiling(2, 0, 4096, 8, 128, 1)
+
+
+def test_autotune_keeps_a_valid_tiling(gpu, oracle):
+    (tile, g0, th, pipe), ms = gpu.tune_dwt(2, 1, 20)
+    assert ms > 0 and th in (256, 512) and (1 << g0) <= tile
+    x = signals.roofline_input(1 << 16, seed=3)
+    w = gpu.transform(x, 14, gpu.DWT, 2, gpu.FWD, 1)
+    ref = oracle.dwt(x, 14, 2)
+    assert np.max(np.abs(w - ref)) / np.max(np.abs(ref)) <= 1e-12

@@ -108,6 +108,9 @@ def lib() -> C.CDLL:
     L.wc_smooth_batch.argtypes = [_dp, C.c_int64, C.POINTER(Signal), C.c_int, C.c_int,
                                   C.POINTER(SignalResult)]
     L.wc_device_status.argtypes = [C.POINTER(C.c_uint)]
+    L.wc_set_dwt_tiling.argtypes = [C.c_int] * 6
+    L.wc_get_dwt_tiling.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.wc_tune_dwt.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.wc_device_count.argtypes = [_ip]
     L.wc_malloc_device.argtypes = [C.POINTER(_vp), C.c_size_t]
     L.wc_free_device.argtypes = [_vp]
@@ -463,6 +466,22 @@ def device_status() -> int:
     v = C.c_uint(0)
     check(lib().wc_device_status(C.byref(v)))
     return v.value
+
+
+def set_dwt_tiling(filt, precision, tile, g0, threads, pipelined):
+    check(lib().wc_set_dwt_tiling(filt, precision, tile, g0, threads, int(pipelined)))
+
+
+def get_dwt_tiling(filt, precision):
+    v = [C.c_int() for _ in range(4)]
+    check(lib().wc_get_dwt_tiling(filt, precision, *[C.byref(x) for x in v]))
+    return tuple(x.value for x in v)
+
+
+def tune_dwt(filt, precision, log2n=24):
+    ms = C.c_float()
+    check(lib().wc_tune_dwt(filt, precision, log2n, C.byref(ms)))
+    return get_dwt_tiling(filt, precision), ms.value
 
 
 def device_count() -> int:

@@ -19,6 +19,7 @@
 // (s,d)[q-j], j < L/2, so the left halo is need_l = ceil(need_{l-1}/2) + L/2-1
 // coefficients at level l.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include <vector>
 
@@ -273,6 +274,234 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     outp[(t0 + m) * ostride] = P::st(SA[m + geo.off[0]]);
 }
 
+// Pipelined first forward pass (S == 1, compact input, contiguous output).
+// A persistent CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...:
+// thread 0 issues the bulk copy of the next tile (and its halo) into the
+// second staging buffer before the block computes the current one, and the
+// previous tile's bulk store drains while the block computes, so loads,
+// stores and arithmetic overlap inside one CTA.  Staging buffers hold T
+// values and are converted to V in place (same size).
+template <int F, class P, int NT>
+__global__ void __launch_bounds__(NT)
+dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
+             typename P::T* __restrict__ out, typename P::T* __restrict__ coarse,
+             unsigned int* status, int64_t ntiles) {
+  using V = typename P::V;
+  using T = typename P::T;
+  static_assert(sizeof(V) == sizeof(T) || std::is_same<V, T>::value, "in-place staging");
+  constexpr int L = filter_len(F);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[2];
+  const int64_t H0 = pad16<T>(fwd_halo(L, G, 0));
+  V* const R0 = reinterpret_cast<V*>(smem_raw);
+  V* const R1 = R0 + pad16<V>(Tt + H0);
+  V* B = R1 + pad16<V>(Tt + H0);
+  V* Z = B + pad16<V>(Tt / 2 + fwd_halo(L, G, 1));
+  int64_t tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  __syncthreads();
+  auto issue = [&](int64_t tl, int b) {
+    const int64_t t0 = tl * Tt;
+    T* dst = reinterpret_cast<T*>(b ? R1 : R0);
+    mbar_expect_tx(&bar[b], (uint32_t)((Tt + H0) * sizeof(T)));
+    if (t0 + Tt + H0 <= N) {
+      bulk_g2s(dst, in + t0, (uint32_t)((Tt + H0) * sizeof(T)), &bar[b]);
+    } else {
+      bulk_g2s(dst, in + t0, (uint32_t)(Tt * sizeof(T)), &bar[b]);
+      if (H0 > 0) bulk_g2s(dst + Tt, in, (uint32_t)(H0 * sizeof(T)), &bar[b]);
+    }
+  };
+  if (threadIdx.x == 0) issue(tile, 0);
+  uint32_t ph0 = 0u, ph1 = 0u;
+  int b = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int64_t t0 = tile * Tt;
+    const int64_t next = tile + gridDim.x;
+    if (threadIdx.x == 0) {
+      if (next < ntiles) issue(next, b ^ 1);
+      bulk_wait_read();  // the previous tile's store has finished reading Z
+    }
+    const bool ok = mbar_wait(b ? &bar[1] : &bar[0], b ? ph1 : ph0, status);
+    if (b) ph1 ^= 1u; else ph0 ^= 1u;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) bulk_wait_read();
+      return;
+    }
+    V* A = b ? R1 : R0;
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+        A[m] = P::ld(reinterpret_cast<const T*>(A)[m]);
+      __syncthreads();
+    }
+    V* src = A;
+    V* dst = B;
+    for (int l = 1; l <= G; l++) {
+      const int64_t nD = Tt >> l;
+      const int64_t nS = nD + fwd_halo(L, G, l);
+      const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
+      for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+        V s, d;
+        fwd_pair<F, P>(src + 2 * k, s, d);
+        dst[k] = s;
+        if (k < nD) Z[doff + k * dstep] = d;
+      }
+      __syncthreads();
+      V* t = src; src = dst; dst = t;
+    }
+    const int64_t nC = Tt >> G;
+    for (int64_t k = threadIdx.x; k < nC; k += blockDim.x) {
+      Z[k << G] = src[k];
+      if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
+    }
+    __syncthreads();
+    T* Zt = reinterpret_cast<T*>(Z);
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+        const V v = Z[m];
+        Zt[m] = P::st(v);
+      }
+    }
+    // Order this thread's generic shared-memory accesses before the async
+    // proxy reads Z (store below) and refills this staging buffer (the load
+    // issued two tiles later).
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_s2g(out + t0, Zt, (uint32_t)(Tt * sizeof(T)));
+      bulk_commit();
+    }
+    b ^= 1;
+  }
+  if (threadIdx.x == 0) bulk_wait_read();
+}
+
+// Pipelined last inverse pass (S == 1): reconstructs tiles of the signal from
+// the interleaved coefficients `det` (the staged range [t0 - H, t0 + Tt) is
+// double-buffered by bulk copies) and the compact level-G scaling values
+// `coarse`; the tile leaves by one bulk store from SA.  Same tile arithmetic
+// as dwt_inv_pass.
+template <int F, class P, int NT>
+__global__ void __launch_bounds__(NT)
+dwt_inv_pipe(const typename P::T* __restrict__ coarse, const typename P::T* __restrict__ det,
+             int64_t N, int G, int64_t Tt, typename P::T* __restrict__ outp, InvGeom geo,
+             unsigned int* status, int64_t ntiles) {
+  using V = typename P::V;
+  using T = typename P::T;
+  constexpr int HH = filter_len(F) / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar[2];
+  const int64_t H = (int64_t)geo.need[G] << G;
+  V* const Z0 = reinterpret_cast<V*>(smem_raw);
+  V* const Z1 = Z0 + pad16<V>(Tt + H);
+  V* SA = Z1 + pad16<V>(Tt + H);
+  V* SB = SA + pad16<V>(Tt + 2 * geo.off[0] + 16);
+  int64_t tile = blockIdx.x;
+  if (tile >= ntiles) return;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  __syncthreads();
+  auto issue = [&](int64_t tl, int b) {
+    const int64_t t0 = tl * Tt;
+    T* dst = reinterpret_cast<T*>(b ? Z1 : Z0);
+    mbar_expect_tx(&bar[b], (uint32_t)((Tt + H) * sizeof(T)));
+    if (t0 >= H) {
+      bulk_g2s(dst, det + (t0 - H), (uint32_t)((Tt + H) * sizeof(T)), &bar[b]);
+    } else {
+      bulk_g2s(dst, det + (N - H), (uint32_t)(H * sizeof(T)), &bar[b]);
+      bulk_g2s(dst + H, det + t0, (uint32_t)(Tt * sizeof(T)), &bar[b]);
+    }
+  };
+  if (threadIdx.x == 0) issue(tile, 0);
+  uint32_t ph0 = 0u, ph1 = 0u;
+  int b = 0;
+  const int64_t NG = N >> G;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int64_t t0 = tile * Tt;
+    const int64_t next = tile + gridDim.x;
+    if (threadIdx.x == 0) {
+      if (next < ntiles) issue(next, b ^ 1);
+      bulk_wait_read();  // the previous tile's store has finished reading SA
+    }
+    const bool ok = mbar_wait(b ? &bar[1] : &bar[0], b ? ph1 : ph0, status);
+    if (b) ph1 ^= 1u; else ph0 ^= 1u;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) bulk_wait_read();
+      return;
+    }
+    V* Z = b ? Z1 : Z0;
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+        Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
+    }
+    {
+      const int64_t q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
+      V* buf = (G & 1) ? SB : SA;
+      for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
+        buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG)]);
+    }
+    __syncthreads();
+    for (int l = G; l >= 1; l--) {
+      V* src = (l & 1) ? SB : SA;
+      V* dst = (l & 1) ? SA : SB;
+      const int P_l = (geo.need[l - 1] + 1) >> 1;
+      const int64_t nq = (Tt >> l) + P_l;
+      const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
+      for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
+        const int64_t qr = k - P_l;
+        V sv[HH], dv[HH];
+#pragma unroll
+        for (int j = 0; j < HH; j++) {
+          sv[j] = src[qr - j + geo.off[l]];
+          dv[j] = Z[(qr - j) * dstep + doff];
+        }
+        V e, o;
+        if constexpr (F == 1) {
+          e = haar_sum<P>(sv[0], dv[0]);
+          o = haar_dif<P>(sv[0], dv[0]);
+        } else {
+          typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+          typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+          ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+          ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+          for (int j = HH - 2; j >= 0; j--) {
+            ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+            ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+            ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+            ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+          }
+          e = P::acc_fin(ae);
+          o = P::acc_fin(ao);
+        }
+        dst[2 * qr + geo.off[l - 1]] = e;
+        dst[2 * qr + 1 + geo.off[l - 1]] = o;
+      }
+      __syncthreads();
+    }
+    T* St = reinterpret_cast<T*>(SA);
+    if constexpr (!std::is_same<T, V>::value) {
+      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+        const V v = SA[m];
+        St[m] = P::st(v);
+      }
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_s2g(outp + t0, St, (uint32_t)(Tt * sizeof(T)));
+      bulk_commit();
+    }
+    b ^= 1;
+  }
+  if (threadIdx.x == 0) bulk_wait_read();
+}
+
 bool aligned16_host(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 struct PassPlan {
@@ -329,13 +558,172 @@ std::vector<PassPlan> plan_passes(int64_t n, int J, int F) {
   return plan;
 }
 
+// ------------------------------------------------------ tile configuration --
+// First-pass tiling of the main DWT path, per (filter, precision): tile size,
+// levels fused in the first pass, threads per CTA and whether the pipelined
+// persistent kernels are used.  Defaults below; wc_tune_dwt() replaces them
+// with the fastest measured candidate.
+struct TileCfg {
+  int tile, g0, threads, pipe;
+};
+
+std::mutex g_cfg_mu;
+TileCfg g_cfg[5][3];
+bool g_cfg_set[5][3] = {};
+
+int gmax_of(int F) { return F == 1 ? 12 : F == 2 ? 8 : F == 3 ? 7 : 6; }
+
+TileCfg default_cfg(int F, int prec) {
+  const int tile = (prec == WC_F32) ? 8192 : 4096;
+  return TileCfg{tile, gmax_of(F), 512, 1};
+}
+
+TileCfg get_cfg(int F, int prec) {
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  if (!g_cfg_set[F][prec]) {
+    g_cfg[F][prec] = default_cfg(F, prec);
+    g_cfg_set[F][prec] = true;
+  }
+  return g_cfg[F][prec];
+}
+
+void set_cfg(int F, int prec, TileCfg c) {
+  std::lock_guard<std::mutex> lk(g_cfg_mu);
+  g_cfg[F][prec] = c;
+  g_cfg_set[F][prec] = true;
+}
+
+template <class P>
+size_t fwd_pipe_smem(int L, int G, int64_t Tt) {
+  using V = typename P::V;
+  using T = typename P::T;
+  return sizeof(V) * (size_t)(2 * pad16<V>(Tt + pad16<T>(fwd_halo(L, G, 0))) +
+                              pad16<V>(Tt / 2 + fwd_halo(L, G, 1)) + pad16<V>(Tt));
+}
+
+template <class P>
+size_t inv_pipe_smem(int L, int G, int64_t Tt) {
+  InvGeom g = inv_geom(L, G);
+  const int64_t H = (int64_t)g.need[G] << G;
+  using V = typename P::V;
+  return sizeof(V) * (size_t)(2 * pad16<V>(Tt + H) + 2 * pad16<V>(Tt + 2 * g.off[0] + 16));
+}
+
+constexpr size_t kPipeSmemMax = 200 * 1024;
+
+// Passes with the first pass taken from cfg; later passes as plan_passes.
+template <class P>
+std::vector<PassPlan> plan_passes_cfg(int64_t n, int J, int F, const TileCfg& c) {
+  const int L = filter_len(F);
+  const int64_t TT = (int64_t)(4096 * 8 / sizeof(typename P::V));
+  const int gmax = gmax_of(F);
+  std::vector<PassPlan> plan;
+  int64_t N = n, S = 1;
+  int l = 0;
+  while (l < J) {
+    const bool first = plan.empty();
+    const int64_t Tt = std::min(N, first ? (int64_t)c.tile : TT);
+    int G = std::min(J - l, (Tt == N) ? 30 : (first ? c.g0 : gmax));
+    auto fits = [&](int g) {
+      if (first && c.pipe && Tt < N)
+        return fwd_pipe_smem<P>(L, g, Tt) <= kPipeSmemMax &&
+               inv_pipe_smem<P>(L, g, Tt) <= kPipeSmemMax;
+      return fwd_smem<P>(L, g, Tt) <= kSmemBudget && inv_smem<P>(L, g, Tt) <= kSmemBudget;
+    };
+    while (G > 1 && ((((int64_t)1 << G) > Tt) || !fits(G))) G--;
+    plan.push_back({N, S, Tt, G});
+    N >>= G;
+    S <<= G;
+    l += G;
+  }
+  return plan;
+}
+
+template <class P>
+constexpr int prec_of() {
+  return std::is_same<P, PExact>::value ? WC_F64_EXACT
+         : std::is_same<P, PDD>::value  ? WC_F64_FAST
+                                        : WC_F32;
+}
+
+int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+// Persistent grid: every CTA that fits at once, at most one per tile.
+template <class K>
+int persistent_grid(K kern, int threads, size_t smem, int64_t ntiles) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem) != cudaSuccess ||
+      per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return (int)std::min<int64_t>(ntiles, (int64_t)per * sm_count());
+}
+
+template <int F, class P, int NT>
+int launch_fwd_pipe_nt(const typename P::T* src, const PassPlan& pp, typename P::T* out,
+                       typename P::T* coarse, unsigned int* status, cudaStream_t s) {
+  const size_t smem = fwd_pipe_smem<P>(filter_len(F), pp.G, pp.Tt);
+  auto kern = dwt_fwd_pipe<F, P, NT>;
+  WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t ntiles = pp.N / pp.Tt;
+  const int grid = persistent_grid(kern, NT, smem, ntiles);
+  {
+    LaunchTimer lt("dwt_fwd_pass0", s);
+    kern<<<grid, NT, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, coarse, status, ntiles);
+  }
+  return after_launch("dwt_fwd_pipe");
+}
+
+template <int F, class P>
+int launch_fwd_pipe(int threads, const typename P::T* src, const PassPlan& pp,
+                    typename P::T* out, typename P::T* coarse, unsigned int* status,
+                    cudaStream_t s) {
+  if (threads == 256) return launch_fwd_pipe_nt<F, P, 256>(src, pp, out, coarse, status, s);
+  return launch_fwd_pipe_nt<F, P, 512>(src, pp, out, coarse, status, s);
+}
+
+template <int F, class P, int NT>
+int launch_inv_pipe_nt(const typename P::T* coarse, const typename P::T* det,
+                       const PassPlan& pp, typename P::T* dst, const InvGeom& geo,
+                       unsigned int* status, cudaStream_t s) {
+  const size_t smem = inv_pipe_smem<P>(filter_len(F), pp.G, pp.Tt);
+  auto kern = dwt_inv_pipe<F, P, NT>;
+  WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t ntiles = pp.N / pp.Tt;
+  const int grid = persistent_grid(kern, NT, smem, ntiles);
+  {
+    LaunchTimer lt("dwt_inv_pass0", s);
+    kern<<<grid, NT, smem, s>>>(coarse, det, pp.N, pp.G, pp.Tt, dst, geo, status, ntiles);
+  }
+  return after_launch("dwt_inv_pipe");
+}
+
+template <int F, class P>
+int launch_inv_pipe(int threads, const typename P::T* coarse, const typename P::T* det,
+                    const PassPlan& pp, typename P::T* dst, const InvGeom& geo,
+                    unsigned int* status, cudaStream_t s) {
+  if (threads == 256) return launch_inv_pipe_nt<F, P, 256>(coarse, det, pp, dst, geo, status, s);
+  return launch_inv_pipe_nt<F, P, 512>(coarse, det, pp, dst, geo, status, s);
+}
+
 template <int F, class P>
 int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream_t s) {
   using T = typename P::T;
   const int L = filter_len(F);
   const T* in = static_cast<const T*>(vin);
   T* out = static_cast<T*>(vout);
-  std::vector<PassPlan> plan = plan_passes<P>(n, J, F);
+  const TileCfg cfg = get_cfg(F, prec_of<P>());
+  std::vector<PassPlan> plan = plan_passes_cfg<P>(n, J, F, cfg);
   unsigned int* status = device_status_word();
   if (!status) return workspace_error();
   const int np = (int)plan.size();
@@ -358,6 +746,11 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       const int64_t H0 = pad16<T>(fwd_halo(L, pp.G, 0));
       const int bulk = aligned16_host(src) && aligned16_host(out) && H0 <= pp.N &&
                        (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
+      if (p == 0 && cfg.pipe && bulk && pp.Tt < pp.N) {
+        WC_TRY((launch_fwd_pipe<F, P>(cfg.threads, src, pp, out, coarse, status, s)));
+        src = coarse;
+        continue;
+      }
       auto kern = dwt_fwd_pass<F, P>;
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       {
@@ -382,6 +775,12 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       const int64_t H = (int64_t)geo.need[pp.G] << pp.G;
       const int bulk = pp.S == 1 && H <= pp.N && aligned16_host(in) && aligned16_host(dst) &&
                        (H * (int64_t)sizeof(T)) % 16 == 0 && (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
+      if (p == 0 && cfg.pipe && bulk && pp.Tt < pp.N) {
+        WC_TRY((launch_inv_pipe<F, P>(cfg.threads, coarse, in, pp, dst, geo, status, s)));
+        coarse = dst;
+        cstride = 1;
+        continue;
+      }
       auto kern = dwt_inv_pass<F, P>;
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       {
@@ -577,4 +976,115 @@ extern "C" int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int
     case WC_F64_FAST: return dispatch_noalloc<PDD>(in, out, len, sense, J, filter, s, base);
     default: return dispatch_noalloc<PF32>(in, out, len, sense, J, filter, s, base);
   }
+}
+
+// ------------------------------------------------------------- autotune --
+
+namespace wc {
+namespace {
+
+int check_cfg(int F, int prec, const TileCfg& c) {
+  if (F < 1 || F > 4 || prec < 0 || prec > 2) return fail(WC_ERR_ARG, "bad filter/precision");
+  if (c.tile < 256 || c.tile > 16384 || (c.tile & (c.tile - 1)) != 0)
+    return fail(WC_ERR_ARG, "tile %d must be a power of two in [256, 16384]", c.tile);
+  if (c.g0 < 1 || c.g0 > 14 || (1 << c.g0) > c.tile)
+    return fail(WC_ERR_ARG, "levels per first pass %d out of range for tile %d", c.g0, c.tile);
+  if (c.threads != 256 && c.threads != 512) return fail(WC_ERR_ARG, "threads must be 256 or 512");
+  return WC_OK;
+}
+
+}  // namespace
+}  // namespace wc
+
+extern "C" int wc_set_dwt_tiling(int filter, int precision, int tile, int g0, int threads,
+                                 int pipelined) {
+  using namespace wc;
+  clear_error();
+  TileCfg c{tile, g0, threads, pipelined ? 1 : 0};
+  WC_TRY(check_cfg(filter, precision, c));
+  set_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_get_dwt_tiling(int filter, int precision, int* tile, int* g0, int* threads,
+                                 int* pipelined) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  const TileCfg c = get_cfg(filter, precision);
+  if (tile) *tile = c.tile;
+  if (g0) *g0 = c.g0;
+  if (threads) *threads = c.threads;
+  if (pipelined) *pipelined = c.pipe;
+  return WC_OK;
+}
+
+// Times forward+inverse DWT (J = log2n - 2 levels, capped at 16) on a random
+// signal of 2^log2n samples for each candidate tiling and keeps the fastest.
+extern "C" int wc_tune_dwt(int filter, int precision, int log2n, float* best_ms) {
+  using namespace wc;
+  clear_error();
+  WC_TRY(ensure_device());
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  if (log2n < 14 || log2n > 28) return fail(WC_ERR_ARG, "log2n must lie in [14, 28]");
+  const int64_t n = (int64_t)1 << log2n;
+  const size_t es = (precision == WC_F32) ? 4 : 8;
+  const int J = std::min(16, check_levels(n, 0, filter_len(filter)));
+  void* a = nullptr;
+  void* b = nullptr;
+  WC_CUDA(cudaMalloc(&a, es * (size_t)n));
+  if (cudaMalloc(&b, es * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(a);
+    return fail(WC_ERR_NOMEM, "tuning buffers");
+  }
+  cudaStream_t s = lib_stream();
+  // any finite data will do: small integers written as bytes
+  cudaMemsetAsync(a, 0x3c, es * (size_t)n, s);
+  const TileCfg keep = get_cfg(filter, precision);
+  const int gm = gmax_of(filter);
+  std::vector<TileCfg> cand;
+  const int tiles8[2] = {2048, 4096}, tiles4[2] = {4096, 8192};
+  for (int ti = 0; ti < 2; ti++) {
+    const int tile = (precision == WC_F32) ? tiles4[ti] : tiles8[ti];
+    for (int g : {gm - 1, gm}) {
+      if (g < 1 || (1 << g) > tile) continue;
+      for (int th : {256, 512})
+        for (int pp : {1, 0}) cand.push_back(TileCfg{tile, g, th, pp});
+    }
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  TileCfg best_c = keep;
+  int rc = WC_OK;
+  for (const TileCfg& c : cand) {
+    set_cfg(filter, precision, c);
+    float ms_min = 1e30f;
+    for (int rep = 0; rep < 4 && rc == WC_OK; rep++) {
+      cudaEventRecord(e0, s);
+      rc = dwt(a, b, n, 1, J, filter, precision, s);
+      if (rc == WC_OK) rc = dwt(b, a, n, 0, J, filter, precision, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) ms_min = std::min(ms_min, ms);
+    }
+    if (rc != WC_OK) break;
+    if (ms_min < best) {
+      best = ms_min;
+      best_c = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(a);
+  cudaFree(b);
+  set_cfg(filter, precision, rc == WC_OK ? best_c : keep);
+  if (best_ms) *best_ms = best;
+  return rc;
 }
