@@ -421,6 +421,8 @@ def profile_case(args):
     a.upload(x)
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
+    if args.tiling:
+        wc.set_dwt_tiling(filt, prec, *[int(v) for v in args.tiling.split(":")])
     for _ in range(2):
         if kind == "dwt":
             wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, min(16, args.log2n - 2), filt, prec, None))
@@ -442,6 +444,8 @@ def main():
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--tiling", default=None,
+                    help="tile:g0:threads:pipelined for --profile-case")
     ap.add_argument("--sweep-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-log2n", type=int, default=24)

@@ -29,20 +29,23 @@ def test_tilings_match_oracle(gpu, oracle, filt, prec):
     keep = gpu.get_dwt_tiling(filt, prec)
     n = 1 << 17
     x = signals.roofline_input(n, seed=filt + 10 * prec)
-    J = min(16, oracle.levels(n, 0, filt))
-    w_ref = oracle.dwt(x, J, filt)
     tol = {0: 0.0, 1: 1e-12, 2: 2e-5}[prec]
     try:
-        for c in candidates(filt, prec):
-            gpu.set_dwt_tiling(filt, prec, *c)
-            w = gpu.transform(x, J, gpu.DWT, filt, gpu.FWD, prec)
-            err = np.max(np.abs(w - w_ref)) / np.max(np.abs(w_ref))
-            assert err <= tol, (c, err)
-            r = gpu.transform(w_ref, J, gpu.DWT, filt, gpu.BWD, prec)
-            if prec == 0:
-                assert np.array_equal(r, oracle.dwt(w_ref, J, filt, P.BWD)), c
-            else:
-                assert np.max(np.abs(r - x)) / np.max(np.abs(x)) <= 4 * tol, c
+        # J = 3: one pass over many tiles (the inverse then reads its coarse
+        # input straight from the interleaved array); J = 16: several passes.
+        for J in (3, min(16, oracle.levels(n, 0, filt))):
+            w_ref = oracle.dwt(x, J, filt)
+            r_ref = oracle.dwt(w_ref, J, filt, P.BWD)
+            for c in candidates(filt, prec):
+                gpu.set_dwt_tiling(filt, prec, *c)
+                w = gpu.transform(x, J, gpu.DWT, filt, gpu.FWD, prec)
+                err = np.max(np.abs(w - w_ref)) / np.max(np.abs(w_ref))
+                assert err <= tol, (J, c, err)
+                r = gpu.transform(w_ref, J, gpu.DWT, filt, gpu.BWD, prec)
+                if prec == 0:
+                    assert np.array_equal(r, r_ref), (J, c)
+                else:
+                    assert np.max(np.abs(r - x)) / np.max(np.abs(x)) <= 4 * tol, (J, c)
         assert gpu.device_status() == 0
     finally:
         gpu.set_dwt_tiling(filt, prec, *keep)

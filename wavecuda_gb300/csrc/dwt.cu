@@ -386,9 +386,10 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
 // as dwt_inv_pass.
 template <int F, class P, int NT>
 __global__ void __launch_bounds__(NT)
-dwt_inv_pipe(const typename P::T* __restrict__ coarse, const typename P::T* __restrict__ det,
-             int64_t N, int G, int64_t Tt, typename P::T* __restrict__ outp, InvGeom geo,
-             unsigned int* status, int64_t ntiles) {
+dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
+             const typename P::T* __restrict__ det, int64_t N, int G, int64_t Tt,
+             typename P::T* __restrict__ outp, InvGeom geo, unsigned int* status,
+             int64_t ntiles) {
   using V = typename P::V;
   using T = typename P::T;
   constexpr int HH = filter_len(F) / 2;
@@ -443,7 +444,7 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, const typename P::T* __re
       const int64_t q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
       V* buf = (G & 1) ? SB : SA;
       for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
-        buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG)]);
+        buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG) * cstride]);
     }
     __syncthreads();
     for (int l = G; l >= 1; l--) {
@@ -693,7 +694,7 @@ int launch_fwd_pipe(int threads, const typename P::T* src, const PassPlan& pp,
 }
 
 template <int F, class P, int NT>
-int launch_inv_pipe_nt(const typename P::T* coarse, const typename P::T* det,
+int launch_inv_pipe_nt(const typename P::T* coarse, int64_t cstride, const typename P::T* det,
                        const PassPlan& pp, typename P::T* dst, const InvGeom& geo,
                        unsigned int* status, cudaStream_t s) {
   const size_t smem = inv_pipe_smem<P>(filter_len(F), pp.G, pp.Tt);
@@ -703,17 +704,19 @@ int launch_inv_pipe_nt(const typename P::T* coarse, const typename P::T* det,
   const int grid = persistent_grid(kern, NT, smem, ntiles);
   {
     LaunchTimer lt("dwt_inv_pass0", s);
-    kern<<<grid, NT, smem, s>>>(coarse, det, pp.N, pp.G, pp.Tt, dst, geo, status, ntiles);
+    kern<<<grid, NT, smem, s>>>(coarse, cstride, det, pp.N, pp.G, pp.Tt, dst, geo, status,
+                                ntiles);
   }
   return after_launch("dwt_inv_pipe");
 }
 
 template <int F, class P>
-int launch_inv_pipe(int threads, const typename P::T* coarse, const typename P::T* det,
-                    const PassPlan& pp, typename P::T* dst, const InvGeom& geo,
-                    unsigned int* status, cudaStream_t s) {
-  if (threads == 256) return launch_inv_pipe_nt<F, P, 256>(coarse, det, pp, dst, geo, status, s);
-  return launch_inv_pipe_nt<F, P, 512>(coarse, det, pp, dst, geo, status, s);
+int launch_inv_pipe(int threads, const typename P::T* coarse, int64_t cstride,
+                    const typename P::T* det, const PassPlan& pp, typename P::T* dst,
+                    const InvGeom& geo, unsigned int* status, cudaStream_t s) {
+  if (threads == 256)
+    return launch_inv_pipe_nt<F, P, 256>(coarse, cstride, det, pp, dst, geo, status, s);
+  return launch_inv_pipe_nt<F, P, 512>(coarse, cstride, det, pp, dst, geo, status, s);
 }
 
 template <int F, class P>
@@ -776,7 +779,7 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       const int bulk = pp.S == 1 && H <= pp.N && aligned16_host(in) && aligned16_host(dst) &&
                        (H * (int64_t)sizeof(T)) % 16 == 0 && (pp.Tt * (int64_t)sizeof(T)) % 16 == 0;
       if (p == 0 && cfg.pipe && bulk && pp.Tt < pp.N) {
-        WC_TRY((launch_inv_pipe<F, P>(cfg.threads, coarse, in, pp, dst, geo, status, s)));
+        WC_TRY((launch_inv_pipe<F, P>(cfg.threads, coarse, cstride, in, pp, dst, geo, status, s)));
         coarse = dst;
         cstride = 1;
         continue;
