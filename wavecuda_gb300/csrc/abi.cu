@@ -253,10 +253,14 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
   float* fa = nullptr;
   float* fb = nullptr;
   if (prec == WC_F32) {
-    char* f = static_cast<char*>(workspace(kSlotConvert, sizeof(float) * (size_t)(nx + nm) + 512));
+    // fa: the transform's FP32 input or output (nm values for MODWT, nx for
+    // DWT); fb: the FP32 signal (nx values).  Both carved from one slot.
+    const size_t abytes = ((sizeof(float) * (size_t)(ttype == 1 ? nm : nx) + 255) / 256) * 256;
+    const size_t bbytes = ((sizeof(float) * (size_t)nx + 255) / 256) * 256;
+    char* f = static_cast<char*>(workspace(kSlotConvert, abytes + bbytes));
     if (!f) return workspace_error();
     fa = reinterpret_cast<float*>(f);
-    fb = reinterpret_cast<float*>(f + ((sizeof(float) * (size_t)(ttype == 1 ? nm : nx) + 255) / 256) * 256);
+    fb = reinterpret_cast<float*>(f + abytes);
   }
   if (ttype == 0) {
     WC_CUDA(cudaMemcpyAsync(A, x, bx, cudaMemcpyHostToDevice, s));
