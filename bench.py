@@ -370,8 +370,96 @@ def ours(args):
         out["sweep"] = sweep
     if tiling:
         out["tiling"] = tiling
+    if not args.no_batch:
+        out["batched"] = batch_bench(wc, args)
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
+
+
+# ------------------------------------------------------- batched smoothing --
+
+def make_batch(wc, nsig, seed):
+    """4096-signal workload: lengths 2^k, k uniform on 10..20; random filter,
+    random transform, J = min(k, 10) clamped to the level limit; universal or
+    CV soft thresholds; signals shaped like doppler/blocks/bumps/heavisine at
+    SNR 3 or 7."""
+    from wavecuda_gb300 import signals as sg
+    rng = np.random.default_rng(seed)
+    shapes = list(sg.SHAPES)
+    sigs, chunks, clean, off = [], [], [], 0
+    for i in range(nsig):
+        k = int(rng.integers(10, 21))
+        n = 1 << k
+        filt = int(rng.integers(1, 5))
+        ttype = int(rng.integers(0, 2))
+        J = min(k, 10, wc.max_levels(n, filt))
+        tt = int(rng.choice([wc.UNIV, wc.CV]))
+        f = sg.SHAPES[shapes[int(rng.integers(0, 4))]](n, i)
+        x = sg.noisy(f, float(rng.choice([3.0, 7.0])), seed=seed * 7919 + i)
+        chunks.append(x)
+        clean.append(f)
+        sigs.append(wc.Signal(off, n, J, ttype, filt, tt, wc.SOFT, 0, J - 1, 0.0, 1e-8))
+        off += n
+    return np.concatenate(chunks), sigs, np.concatenate(clean)
+
+
+def batch_bench(wc, args):
+    import ctypes as C
+    L = wc.lib()
+    data, sigs, clean = make_batch(wc, args.batch_signals, seed=11)
+    out = {"workload": f"{len(sigs)} signals, n = 2^k, k ~ U{{10..20}}, random filter/transform, "
+                       "J = min(k, 10) clamped, universal or CV soft, tol 1e-8",
+           "samples": int(data.size)}
+    rng = np.random.default_rng(5)
+    sub = sorted(rng.choice(len(sigs), size=min(args.plain_signals, len(sigs)), replace=False))
+    for prec in (1, 2):
+        r = {}
+        arr = (wc.Signal * len(sigs))(*sigs)
+        plan = C.c_void_p()
+        wc.check(L.wc_batch_plan_create(arr, len(sigs), prec, C.byref(plan)))
+        buf = wc.DeviceBuffer(8 * data.size)
+        buf.upload(data)
+        ms_tune = C.c_float()
+        wc.check(L.wc_batch_autotune(plan, buf.ptr, C.byref(ms_tune)))
+        grid = C.c_int()
+        wc.check(L.wc_batch_plan_info(plan, C.byref(grid), None))
+        s = wc.default_stream()
+        e0, e1 = wc.Event(), wc.Event()
+        buf.upload(data, s)
+        e0.record(s)
+        wc.check(L.wc_batch_run_device(plan, buf.ptr, s))
+        e1.record(s)
+        wc.check(L.wc_stream_synchronize(s))
+        dev_ms = e0.elapsed_ms(e1)
+        y = buf.download(np.float64, data.size, s)
+        res = (wc.SignalResult * len(sigs))()
+        wc.check(L.wc_batch_results(plan, res, s))
+        wc.check(L.wc_batch_plan_destroy(plan))
+        buf.free()
+        # end to end through the host-buffer batch call
+        t0 = time.perf_counter()
+        y2, _ = wc.smooth_batch(data, sigs, prec)
+        e2e_s = time.perf_counter() - t0
+        mse = float(np.mean((y - clean) ** 2))
+        # plain per-signal path on a random subsample
+        t0 = time.perf_counter()
+        for i in sub:
+            sg_ = sigs[i]
+            x = data[sg_.offset:sg_.offset + sg_.len]
+            wc.smooth(x, sg_.nlevels, sg_.ttype, sg_.filter, sg_.threshtype, 0.0, sg_.hardness,
+                      sg_.minlevel, sg_.maxlevel, sg_.tol, prec)
+        plain_s = time.perf_counter() - t0
+        r["batched_signals_s"] = len(sigs) / (dev_ms / 1e3)
+        r["batched_device_ms"] = dev_ms
+        r["batched_e2e_signals_s"] = len(sigs) / e2e_s
+        r["plain_signals_s"] = len(sub) / plain_s
+        r["plain_sample"] = f"{len(sub)} random signals of the batch, one wc_smooth call each"
+        r["speedup_e2e"] = r["batched_e2e_signals_s"] / r["plain_signals_s"]
+        r["grid"] = grid.value
+        r["mse_vs_clean"] = mse
+        r["cv_iterations_mean"] = float(np.mean([x.iterations for x in res if x.iterations]))
+        out[PREC[prec]] = r
+    return out
 
 
 def reference(args):
@@ -444,6 +532,9 @@ def main():
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-signals", type=int, default=4096)
+    ap.add_argument("--plain-signals", type=int, default=96)
     ap.add_argument("--tiling", default=None,
                     help="tile:g0:threads:pipelined for --profile-case")
     ap.add_argument("--sweep-steps", type=int, default=2)
