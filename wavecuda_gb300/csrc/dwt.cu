@@ -65,117 +65,6 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
   }
 }
 
-// Two adjacent values moved as one 16-byte (two floats: 8-byte) shared-memory
-// access.  Every level buffer starts on a 16-byte boundary (pad16 regions).
-template <class V>
-struct __align__(2 * sizeof(V)) Two {
-  V a, b;
-};
-
-constexpr int kR = 4;  // output pairs per thread and iteration
-
-// One forward level inside a tile: src holds 2*nS + L - 2 values (nIn), dst
-// receives the nS scaling values and Z the nD details at doff + k*dstep.
-// Each thread takes kR consecutive pairs, so the L-2 inputs that neighbouring
-// pairs share are read once; full groups use vector accesses, the tail group
-// guarded scalar ones.
-template <int F, class P>
-__device__ __forceinline__ void fwd_level(const typename P::V* __restrict__ src, int nIn,
-                                          typename P::V* __restrict__ dst,
-                                          typename P::V* __restrict__ Z, int nS, int nD,
-                                          int dstep, int doff) {
-  using V = typename P::V;
-  constexpr int L = filter_len(F);
-  constexpr int NV = 2 * kR + L - 2;  // even
-  for (int k0 = kR * (int)threadIdx.x; k0 < nS; k0 += kR * (int)blockDim.x) {
-    V v[NV];
-    const bool full = (k0 + kR <= nS);
-    if (full) {
-      const Two<V>* s2 = reinterpret_cast<const Two<V>*>(src + 2 * k0);
-#pragma unroll
-      for (int j = 0; j < NV / 2; j++) {
-        const Two<V> t = s2[j];
-        v[2 * j] = t.a;
-        v[2 * j + 1] = t.b;
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < NV; j++) v[j] = (2 * k0 + j < nIn) ? src[2 * k0 + j] : v[0];
-    }
-    V sv[kR];
-#pragma unroll
-    for (int r = 0; r < kR; r++) {
-      V d;
-      fwd_pair<F, P>(v + 2 * r, sv[r], d);
-      const int k = k0 + r;
-      if (k < nD) Z[doff + k * dstep] = d;
-    }
-    if (full) {
-      Two<V>* d2 = reinterpret_cast<Two<V>*>(dst + k0);
-#pragma unroll
-      for (int r = 0; r < kR / 2; r++) d2[r] = Two<V>{sv[2 * r], sv[2 * r + 1]};
-    } else {
-#pragma unroll
-      for (int r = 0; r < kR; r++)
-        if (k0 + r < nS) dst[k0 + r] = sv[r];
-    }
-  }
-}
-
-// One inverse level: output pairs k in [0, nq), q = k - P_l relative to the
-// tile; s values at src[q - j + offs], details at Z[(q - j)*dstep + doff]
-// (j < L/2); writes dst[2q + offd] and dst[2q + 1 + offd] (offd even).
-template <int F, class P>
-__device__ __forceinline__ void inv_level(const typename P::V* __restrict__ src,
-                                          const typename P::V* __restrict__ Z,
-                                          typename P::V* __restrict__ dst, int nq, int P_l,
-                                          int offs, int offd, int dstep, int doff) {
-  using V = typename P::V;
-  constexpr int HH = filter_len(F) / 2;
-  constexpr int NV = kR + HH - 1;
-  for (int k0 = kR * (int)threadIdx.x; k0 < nq; k0 += kR * (int)blockDim.x) {
-    const int base = k0 - P_l - (HH - 1);  // q of sv[0]
-    const int nvalid = nq - k0 + HH - 1;   // sv[j] valid for j < nvalid
-    V sv[NV], dv[NV];
-#pragma unroll
-    for (int j = 0; j < NV; j++) {
-      if (j < nvalid) {
-        sv[j] = src[base + j + offs];
-        dv[j] = Z[(base + j) * dstep + doff];
-      } else {
-        sv[j] = sv[0];
-        dv[j] = dv[0];
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < kR; r++) {
-      if (k0 + r >= nq) break;
-      // q = base + r + HH - 1; its j-th left neighbour is sv[r + HH - 1 - j]
-      V e, o;
-      if constexpr (F == 1) {
-        e = haar_sum<P>(sv[r], dv[r]);
-        o = haar_dif<P>(sv[r], dv[r]);
-      } else {
-        typename P::Acc ae = P::acc_init(sv[r], tap_h(F, 2 * (HH - 1)));
-        typename P::Acc ao = P::acc_init(sv[r], tap_h(F, 2 * (HH - 1) + 1));
-        ae = P::acc_add(ae, dv[r], tap_g(F, 2 * (HH - 1)));
-        ao = P::acc_add(ao, dv[r], tap_g(F, 2 * (HH - 1) + 1));
-#pragma unroll
-        for (int j = HH - 2; j >= 0; j--) {
-          ae = P::acc_add(ae, sv[r + HH - 1 - j], tap_h(F, 2 * j));
-          ao = P::acc_add(ao, sv[r + HH - 1 - j], tap_h(F, 2 * j + 1));
-          ae = P::acc_add(ae, dv[r + HH - 1 - j], tap_g(F, 2 * j));
-          ao = P::acc_add(ao, dv[r + HH - 1 - j], tap_g(F, 2 * j + 1));
-        }
-        e = P::acc_fin(ae);
-        o = P::acc_fin(ao);
-      }
-      const int q = base + r + HH - 1;
-      *reinterpret_cast<Two<V>*>(dst + 2 * q + offd) = Two<V>{e, o};
-    }
-  }
-}
-
 // Forward pass.  y[m] = in[m] (m < N, compact).  Writes the tile's
 // interleaved result to out[(t0+m)*S] and its level-G scaling values to
 // coarse[t0/2^G + k] (when coarse != nullptr).  With `bulk` set, the tile and
@@ -229,8 +118,12 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     const int64_t nD = Tt >> l;
     const int64_t nS = nD + fwd_halo(L, G, l);
     const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
-    fwd_level<F, P>(src, (int)((Tt >> (l - 1)) + fwd_halo(L, G, l - 1)), dst, Z, (int)nS, (int)nD,
-                      (int)dstep, (int)doff);
+    for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+      V s, d;
+      fwd_pair<F, P>(src + 2 * k, s, d);
+      dst[k] = s;
+      if (k < nD) Z[doff + k * dstep] = d;
+    }
     __syncthreads();
     V* t = src; src = dst; dst = t;
   }
@@ -326,7 +219,38 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     const int P_l = (geo.need[l - 1] + 1) >> 1;
     const int64_t nq = (Tt >> l) + P_l;
     const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
-    inv_level<F, P>(src, Z, dst, (int)nq, P_l, geo.off[l], geo.off[l - 1], (int)dstep, (int)doff);
+    for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
+      const int64_t qr = k - P_l;  // q - q0
+      constexpr int HH = filter_len(F) / 2;
+      V sv[HH], dv[HH];
+#pragma unroll
+      for (int j = 0; j < HH; j++) {
+        sv[j] = src[qr - j + geo.off[l]];
+        dv[j] = Z[(qr - j) * dstep + doff];
+      }
+      V e, o;
+      // inv_pair addresses s[-j] / d[-j]; sv/dv are stored in ascending j.
+      if constexpr (F == 1) {
+        e = haar_sum<P>(sv[0], dv[0]);
+        o = haar_dif<P>(sv[0], dv[0]);
+      } else {
+        typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+        typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+        ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+        ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+        for (int j = HH - 2; j >= 0; j--) {
+          ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+          ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+          ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+          ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+        }
+        e = P::acc_fin(ae);
+        o = P::acc_fin(ao);
+      }
+      dst[2 * qr + geo.off[l - 1]] = e;
+      dst[2 * qr + 1 + geo.off[l - 1]] = o;
+    }
     __syncthreads();
   }
   if (bulk && ostride == 1) {
@@ -419,8 +343,12 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
       const int64_t nD = Tt >> l;
       const int64_t nS = nD + fwd_halo(L, G, l);
       const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
-      fwd_level<F, P>(src, (int)((Tt >> (l - 1)) + fwd_halo(L, G, l - 1)), dst, Z, (int)nS, (int)nD,
-                      (int)dstep, (int)doff);
+      for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+        V s, d;
+        fwd_pair<F, P>(src + 2 * k, s, d);
+        dst[k] = s;
+        if (k < nD) Z[doff + k * dstep] = d;
+      }
       __syncthreads();
       V* t = src; src = dst; dst = t;
     }
@@ -464,6 +392,7 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
              int64_t ntiles) {
   using V = typename P::V;
   using T = typename P::T;
+  constexpr int HH = filter_len(F) / 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar[2];
   const int64_t H = (int64_t)geo.need[G] << G;
@@ -524,7 +453,36 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
       const int P_l = (geo.need[l - 1] + 1) >> 1;
       const int64_t nq = (Tt >> l) + P_l;
       const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
-      inv_level<F, P>(src, Z, dst, (int)nq, P_l, geo.off[l], geo.off[l - 1], (int)dstep, (int)doff);
+      for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
+        const int64_t qr = k - P_l;
+        V sv[HH], dv[HH];
+#pragma unroll
+        for (int j = 0; j < HH; j++) {
+          sv[j] = src[qr - j + geo.off[l]];
+          dv[j] = Z[(qr - j) * dstep + doff];
+        }
+        V e, o;
+        if constexpr (F == 1) {
+          e = haar_sum<P>(sv[0], dv[0]);
+          o = haar_dif<P>(sv[0], dv[0]);
+        } else {
+          typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+          typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+          ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+          ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+          for (int j = HH - 2; j >= 0; j--) {
+            ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+            ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+            ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+            ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+          }
+          e = P::acc_fin(ae);
+          o = P::acc_fin(ao);
+        }
+        dst[2 * qr + geo.off[l - 1]] = e;
+        dst[2 * qr + 1 + geo.off[l - 1]] = o;
+      }
       __syncthreads();
     }
     T* St = reinterpret_cast<T*>(SA);
