@@ -10,11 +10,21 @@
 // inverse reads s_J and d_1..d_J only and keeps its intermediate scaling
 // sequences in workspace, so xmod is not modified.
 //
-// Each level is one streaming launch: thread i produces S[i], D[i] (or X[i])
-// from L taps spaced 2^l apart.  Loads of neighbouring threads are
-// contiguous, so every tap read is coalesced and the L-fold reuse of a value
-// is served from L1/L2.
+// Row view.  A level whose taps are d = 2^l0 apart splits the signal into d
+// interleaved sequences: element (m, r) = x[r + m d], r < d, m < n/d, and the
+// taps of (m, r) are rows m + k (forward) or m - k (inverse) of the same
+// column.  The next level's taps are rows m + 2k, and so on.  A CTA stages a
+// tile of C adjacent columns (C = min(d, 32): each row segment is contiguous
+// in memory) by M + halo rows in shared memory, converting each value once,
+// and runs several levels inside the tile; only the levels' outputs (and,
+// for the inverse, the group's final scaling sequence) touch HBM.  The
+// forward fuses NF levels (halo (L-1)(2^NF - 1) rows to the right); the
+// inverse fuses NI levels (halo (L-1)(2^NI - 1) rows to the left), so its
+// traffic is NI + 2 sequences per NI levels instead of 3 per level.  Every
+// output is computed with the reference's term order, so WC_F64_EXACT stays
+// bit-identical however the levels are grouped.
 #include <algorithm>
+#include <type_traits>
 
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
@@ -24,66 +34,224 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Forward analysis of one output from taps v[k * stride], k < L.
 template <int F, class P>
-__global__ void __launch_bounds__(kThreads)
-modwt_fwd_level(const typename P::T* __restrict__ X, typename P::T* __restrict__ S,
-                typename P::T* __restrict__ D, int64_t n, int64_t skip) {
-  using V = typename P::V;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    if constexpr (F == 1) {
-      V a = P::ld(X[i]), b = P::ld(X[wrap(i + skip, n)]);
-      D[i] = P::st(haar_dif<P>(a, b));
-      S[i] = P::st(haar_sum<P>(a, b));
-    } else {
-      constexpr int L = filter_len(F);
-      V v = P::ld(X[i]);
-      typename P::Acc d = P::acc_init(v, tap_g(F, 0)), s = P::acc_init(v, tap_h(F, 0));
+__device__ __forceinline__ void fwd_taps(const typename P::V* v, int stride, typename P::V& s,
+                                         typename P::V& d) {
+  if constexpr (F == 1) {
+    s = haar_sum<P>(v[0], v[stride]);
+    d = haar_dif<P>(v[0], v[stride]);
+  } else {
+    constexpr int L = filter_len(F);
+    typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
+    typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
 #pragma unroll
-      for (int k = 1; k < L; k++) {
-        v = P::ld(X[wrap(i + (int64_t)k * skip, n)]);
-        d = P::acc_add(d, v, tap_g(F, k));
-        s = P::acc_add(s, v, tap_h(F, k));
-      }
-      D[i] = P::st(P::acc_fin(d));
-      S[i] = P::st(P::acc_fin(s));
+    for (int k = 1; k < L; k++) {
+      ad = P::acc_add(ad, v[k * stride], tap_g(F, k));
+      as = P::acc_add(as, v[k * stride], tap_h(F, k));
+    }
+    d = P::acc_fin(ad);
+    s = P::acc_fin(as);
+  }
+}
+
+// Inverse synthesis of one output from S[-k * stride], D[-k * stride].
+template <int F, class P>
+__device__ __forceinline__ typename P::V inv_taps(const typename P::V* S, const typename P::V* D,
+                                                   int stride) {
+  if constexpr (F == 1) {
+    typename P::V acc = P::add(S[0], D[0]);
+    acc = P::add(acc, S[-stride]);
+    acc = P::sub(acc, D[-stride]);
+    return P::mul(acc, kHInvR2);
+  } else {
+    constexpr int L = filter_len(F);
+    typename P::Acc acc;
+#pragma unroll
+    for (int t = 0; t < L; t++) {
+      // even taps L-2, ..., 0 then odd taps L-1, ..., 1
+      const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
+      if (t == 0) acc = P::acc_init(S[-k * stride], tap_h(F, k));
+      else acc = P::acc_add(acc, S[-k * stride], tap_h(F, k));
+      acc = P::acc_add(acc, D[-k * stride], tap_g(F, k));
+    }
+    return P::half(P::acc_fin(acc));
+  }
+}
+
+// Forward levels l0 .. l0+NF-1.  Tile: columns r0 .. r0+C-1, rows m0 ..
+// m0+M-1 of the row view with unit d0 = 2^l0 (nrows = n / d0 rows).
+template <int F, class P, int NF>
+__global__ void __launch_bounds__(kThreads)
+modwt_fwd_tiled(const typename P::T* __restrict__ X, typename P::T* __restrict__ xmod,
+                int64_t n, int l0, int C, int M) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  constexpr int HR = (L - 1) * ((1 << NF) - 1);       // input halo rows
+  constexpr int H1 = (NF == 2) ? 2 * (L - 1) : 0;     // extra level-l0 rows kept
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* In = reinterpret_cast<V*>(smem_raw);
+  V* S1 = In + (M + HR) * C;
+  const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
+  const int64_t nb = d0 / C;
+  const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
+  const int cs = __ffs(C) - 1;  // C is a power of two
+  const int tot = (M + HR) * C;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int row = e >> cs, c = e & (C - 1);
+    In[e] = P::ld(X[(r0 + c) + ((m0 + row) & (nrows - 1)) * d0]);
+  }
+  __syncthreads();
+  typename P::T* S0 = xmod + (int64_t)2 * l0 * n;
+  typename P::T* D0 = S0 + n;
+  const int rows1 = M + H1;
+  for (int e = threadIdx.x; e < rows1 * C; e += blockDim.x) {
+    const int row = e >> cs, c = e & (C - 1);
+    V s, d;
+    fwd_taps<F, P>(In + e, C, s, d);
+    if (row < M) {
+      const int64_t g = (r0 + c) + (m0 + row) * d0;
+      S0[g] = P::st(s);
+      D0[g] = P::st(d);
+    }
+    if constexpr (NF == 2) S1[e] = s;
+  }
+  if constexpr (NF == 2) {
+    __syncthreads();
+    typename P::T* S2 = S0 + 2 * n;
+    typename P::T* D2 = S2 + n;
+    for (int e = threadIdx.x; e < M * C; e += blockDim.x) {
+      const int row = e >> cs, c = e & (C - 1);
+      V s, d;
+      fwd_taps<F, P>(S1 + e, 2 * C, s, d);
+      const int64_t g = (r0 + c) + (m0 + row) * d0;
+      S2[g] = P::st(s);
+      D2[g] = P::st(d);
     }
   }
 }
 
-template <int F, class P>
+// Inverse levels l0+NI-1 down to l0 (row unit d0 = 2^l0).  Stop holds the
+// scaling sequence the group starts from (s block of level l0+NI-1, or the
+// previous group's output); the detail blocks come from xmod; out receives
+// the group's reconstruction for rows m0 .. m0+M-1.  Array row a of the tile
+// is global row m0 - HR + a (periodic).
+template <int F, class P, int NI>
 __global__ void __launch_bounds__(kThreads)
-modwt_inv_level(typename P::T* __restrict__ Xout, const typename P::T* __restrict__ S,
-                const typename P::T* __restrict__ D, int64_t n, int64_t skip) {
+modwt_inv_tiled(const typename P::T* __restrict__ Stop, const typename P::T* __restrict__ xmod,
+                typename P::T* __restrict__ out, int64_t n, int l0, int C, int M) {
   using V = typename P::V;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    if constexpr (F == 1) {
-      const int64_t j = wrap(i - skip, n);
-      V acc = P::add(P::ld(S[i]), P::ld(D[i]));
-      acc = P::add(acc, P::ld(S[j]));
-      acc = P::sub(acc, P::ld(D[j]));
-      Xout[i] = P::st(P::mul(acc, kHInvR2));
-    } else {
-      constexpr int L = filter_len(F);
-      typename P::Acc acc;
+  constexpr int L = filter_len(F);
+  constexpr int HR = (L - 1) * ((1 << NI) - 1);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int R = M + HR;
+  V* St = reinterpret_cast<V*>(smem_raw);
+  V* Db = St + R * C;           // NI detail tiles
+  V* A = Db + NI * R * C;       // intermediates (NI > 1)
+  V* B = A + R * C;
+  const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
+  const int64_t nb = d0 / C;
+  const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
+  const int cs = __ffs(C) - 1;
+  const int tot = R * C;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int row = e >> cs, c = e & (C - 1);
+    const int64_t g = (r0 + c) + ((m0 - HR + row) & (nrows - 1)) * d0;
+    St[e] = P::ld(Stop[g]);
 #pragma unroll
-      for (int t = 0; t < L; t++) {
-        // even taps L-2, ..., 0 then odd taps L-1, ..., 1
-        const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
-        const int64_t j = wrap(i - (int64_t)k * skip, n);
-        if (t == 0) acc = P::acc_init(P::ld(S[j]), tap_h(F, k));
-        else acc = P::acc_add(acc, P::ld(S[j]), tap_h(F, k));
-        acc = P::acc_add(acc, P::ld(D[j]), tap_g(F, k));
+    for (int t = 0; t < NI; t++)
+      Db[t * tot + e] = P::ld(xmod[(int64_t)(2 * (l0 + t) + 1) * n + g]);
+  }
+  __syncthreads();
+  const V* cur = St;
+#pragma unroll
+  for (int t = NI - 1; t >= 0; t--) {
+    const int rd = 1 << t;
+    const int a_lo = HR - (L - 1) * ((1 << t) - 1);
+    V* dst = ((NI - 1 - t) & 1) ? B : A;
+    const V* Dt = Db + t * tot;
+    for (int e = a_lo * C + threadIdx.x; e < tot; e += blockDim.x) {
+      const V v = inv_taps<F, P>(cur + e, Dt + e, rd * C);
+      if (t == 0) {
+        const int row = e >> cs, c = e & (C - 1);
+        out[(r0 + c) + (m0 - HR + row) * d0] = P::st(v);
+      } else {
+        dst[e] = v;
       }
-      Xout[i] = P::st(P::half(P::acc_fin(acc)));
+    }
+    if (t > 0) {
+      __syncthreads();
+      cur = dst;
     }
   }
 }
 
-unsigned grid_for(int64_t n) {
-  int64_t blocks = (n + kThreads - 1) / kThreads;
-  return (unsigned)std::min<int64_t>(blocks, 152 * 16);
+template <class P>
+struct Geo {
+  int C, M;
+  size_t smem;
+};
+
+constexpr size_t kTileSmem = 96 * 1024;
+
+// Tile shape for level unit d0: C = min(d0, 32) columns and the largest
+// power-of-two row count M <= nrows with C*M <= target whose shared memory
+// fits the budget.
+template <class P>
+Geo<P> tile_geo(int64_t n, int l0, int halo, int arrays, int lead_rows) {
+  using V = typename P::V;
+  const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
+  const int C = (int)std::min<int64_t>(d0, 32);
+  const int target = (sizeof(V) == 4) ? 4096 : 2048;
+  int M = (int)std::min<int64_t>(nrows, std::max(1, target / C));
+  auto bytes = [&](int m) {
+    return sizeof(V) * (size_t)C * (size_t)((m + halo) * arrays + lead_rows);
+  };
+  while (M > 1 && bytes(M) > kTileSmem) M >>= 1;
+  return {C, M, bytes(M)};
+}
+
+constexpr int nf_max(int F) { return 2; }
+constexpr int ni_max(int F) { return F == 1 ? 3 : 2; }
+
+template <int F, class P, int NF>
+int launch_fwd(const typename P::T* X, typename P::T* xmod, int64_t n, int l0, cudaStream_t s) {
+  constexpr int L = filter_len(F);
+  constexpr int HR = (L - 1) * ((1 << NF) - 1);
+  // In: M + HR rows; S1 (NF == 2): M + 2(L-1) rows.
+  Geo<P> g = tile_geo<P>(n, l0, HR, 1, NF == 2 ? 0 : 0);
+  if (NF == 2) {
+    // recompute with both arrays
+    using V = typename P::V;
+    while (g.M > 1 && sizeof(V) * (size_t)g.C * (size_t)((g.M + HR) + (g.M + 2 * (L - 1))) > kTileSmem)
+      g.M >>= 1;
+    g.smem = sizeof(V) * (size_t)g.C * (size_t)((g.M + HR) + (g.M + 2 * (L - 1)));
+  }
+  auto kern = modwt_fwd_tiled<F, P, NF>;
+  WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
+  const int64_t blocks = (((int64_t)1 << l0) / g.C) * ((n >> l0) / g.M);
+  {
+    LaunchTimer lt("modwt_fwd_tiled", s);
+    kern<<<(unsigned)blocks, kThreads, g.smem, s>>>(X, xmod, n, l0, g.C, g.M);
+  }
+  return after_launch("modwt_fwd_tiled");
+}
+
+template <int F, class P, int NI>
+int launch_inv(const typename P::T* Stop, const typename P::T* xmod, typename P::T* out,
+               int64_t n, int l0, cudaStream_t s) {
+  constexpr int L = filter_len(F);
+  constexpr int HR = (L - 1) * ((1 << NI) - 1);
+  const int arrays = 1 + NI + (NI > 1 ? 2 : 0);
+  Geo<P> g = tile_geo<P>(n, l0, HR, arrays, 0);
+  auto kern = modwt_inv_tiled<F, P, NI>;
+  WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
+  const int64_t blocks = (((int64_t)1 << l0) / g.C) * ((n >> l0) / g.M);
+  {
+    LaunchTimer lt("modwt_inv_tiled", s);
+    kern<<<(unsigned)blocks, kThreads, g.smem, s>>>(Stop, xmod, out, n, l0, g.C, g.M);
+  }
+  return after_launch("modwt_inv_tiled");
 }
 
 template <int F, class P>
@@ -91,35 +259,33 @@ int run_modwt(void* vx, void* vxmod, int64_t n, int sense, int J, cudaStream_t s
   using T = typename P::T;
   T* x = static_cast<T*>(vx);
   T* xmod = static_cast<T*>(vxmod);
-  const unsigned grid = grid_for(n);
   if (sense == 1) {
-    for (int l = 0; l < J; l++) {
+    for (int l = 0; l < J;) {
       const T* X = (l == 0) ? x : xmod + (int64_t)2 * (l - 1) * n;
-      {
-        LaunchTimer lt("modwt_fwd_level", s);
-        modwt_fwd_level<F, P><<<grid, kThreads, 0, s>>>(
-            X, xmod + (int64_t)2 * l * n, xmod + (int64_t)(2 * l + 1) * n, n, (int64_t)1 << l);
-      }
-      WC_TRY(after_launch("modwt_fwd_level"));
+      const int nf = std::min(nf_max(F), J - l);
+      if (nf == 2) WC_TRY((launch_fwd<F, P, 2>(X, xmod, n, l, s)));
+      else WC_TRY((launch_fwd<F, P, 1>(X, xmod, n, l, s)));
+      l += nf;
     }
     return WC_OK;
   }
   T* tmp[2] = {nullptr, nullptr};
-  if (J > 1) {
+  if (J > ni_max(F)) {
     tmp[0] = static_cast<T*>(workspace(kSlotModwt0, sizeof(T) * (size_t)n));
     tmp[1] = static_cast<T*>(workspace(kSlotModwt1, sizeof(T) * (size_t)n));
     if (!tmp[0] || !tmp[1]) return workspace_error();
   }
-  const T* Sin = xmod + (int64_t)2 * (J - 1) * n;
-  for (int l = J - 1; l >= 0; l--) {
-    T* out = (l == 0) ? x : tmp[l & 1];
-    {
-      LaunchTimer lt("modwt_inv_level", s);
-      modwt_inv_level<F, P><<<grid, kThreads, 0, s>>>(out, Sin, xmod + (int64_t)(2 * l + 1) * n,
-                                                      n, (int64_t)1 << l);
-    }
-    WC_TRY(after_launch("modwt_inv_level"));
-    Sin = out;
+  const T* Stop = xmod + (int64_t)2 * (J - 1) * n;
+  int g = 0;
+  for (int hi = J - 1; hi >= 0; g++) {
+    const int ni = std::min(ni_max(F), hi + 1);
+    const int l0 = hi - ni + 1;
+    T* out = (l0 == 0) ? x : tmp[g & 1];
+    if (ni == 3) WC_TRY((launch_inv<F, P, 3>(Stop, xmod, out, n, l0, s)));
+    else if (ni == 2) WC_TRY((launch_inv<F, P, 2>(Stop, xmod, out, n, l0, s)));
+    else WC_TRY((launch_inv<F, P, 1>(Stop, xmod, out, n, l0, s)));
+    Stop = out;
+    hi = l0 - 1;
   }
   return WC_OK;
 }
