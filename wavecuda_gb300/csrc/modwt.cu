@@ -97,6 +97,8 @@ modwt_fwd_tiled(const typename P::T* __restrict__ X, typename P::T* __restrict__
   const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
   const int cs = __ffs(C) - 1;  // C is a power of two
   const int tot = (M + HR) * C;
+  // Unrolled so that each thread keeps several independent loads in flight.
+#pragma unroll 8
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const int row = e >> cs, c = e & (C - 1);
     In[e] = P::ld(X[(r0 + c) + ((m0 + row) & (nrows - 1)) * d0]);
@@ -154,6 +156,7 @@ modwt_inv_tiled(const typename P::T* __restrict__ Stop, const typename P::T* __r
   const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
   const int cs = __ffs(C) - 1;
   const int tot = R * C;
+#pragma unroll 4
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const int row = e >> cs, c = e & (C - 1);
     const int64_t g = (r0 + c) + ((m0 - HR + row) & (nrows - 1)) * d0;
