@@ -245,6 +245,57 @@ WC_API int wc_median_mad_device(const double* data, int64_t n, double* median, d
  * Computed in parallel; synchronous; the sum is returned on the host. */
 WC_API int wc_sequential_sum_device(const double* terms, int64_t n, double* sum, void* stream);
 
+/* ---- differentiation (no counterpart in the reference; backward calls for
+ * gradient-based threshold tuning).  FP64 device vectors; `sense` names the
+ * operator whose adjoint is applied (1 = the forward transform, 0 = the
+ * inverse), so gin is the cotangent of that operator's output and gout the
+ * cotangent of its input. */
+
+/* DWT: adjoint(forward) is the inverse and adjoint(inverse) the forward
+ * (the periodic orthonormal DWT is its own transpose pair). */
+WC_API int wc_dwt_adjoint_device(const void* gin, void* gout, int64_t len, int sense, int nlevels,
+                                 int filter, int precision, void* stream);
+
+/* Time-ordered MODWT (FP64).  sense 1: gxmod (2*nlevels*len cotangents of
+ * every stored block, s_l and d_l of each level) -> gx (len).  sense 0: gx
+ * (cotangent of a reconstruction) -> gxmod (cotangents of s_J and d_1..d_J;
+ * zero for the intermediate s blocks, which the inverse does not read). */
+WC_API int wc_modwt_adjoint_device(double* gx, double* gxmod, int64_t len, int sense, int nlevels,
+                                   int filter, void* stream);
+
+/* Soft thresholding with one threshold per level (lambda: host array of
+ * nlevels values, levels [minlevel, maxlevel], 0-based) on a DWT
+ * (ttype 0) or MODWT (ttype 1) coefficient vector `coef`.  Given the
+ * cotangent `gout` of the thresholded vector, writes gcoef (optional, same
+ * length) and glambda (device, nlevels values, overwritten):
+ * d eta/dc = 1{|c| >= t}, d eta/dt = -sign(c) 1{|c| >= t}. */
+WC_API int wc_soft_threshold_adjoint_device(const double* coef, const double* gout, double* gcoef,
+                                            double* glambda, int64_t len, int nlevels, int ttype,
+                                            const double* lambda, int minlevel, int maxlevel,
+                                            void* stream);
+
+/* Loss of per-level soft thresholds and its gradient, for one FP64 signal x
+ * (device).  lambda and grad are host arrays of nlevels values (levels
+ * outside [minlevel, maxlevel] get gradient 0).
+ *   WC_LOSS_SURE: Stein's unbiased risk estimate of the smoothed signal,
+ *     ||f - x||^2 - n sigma^2 + 2 sigma^2 div f, where the divergence counts
+ *     kept coefficients weighted by the per-level trace of synthesis times
+ *     analysis (1 for the DWT, 2^-(l+1) for the MODWT).  The kept indicator
+ *     is replaced by a logistic step of width eps (eps 0: the indicator, whose
+ *     derivative is 0).  sigma <= 0: estimated as the MAD of the finest
+ *     details; the value used is returned in *sigma_used (optional).
+ *   WC_LOSS_CV: the two-fold cross-validation loss of interp_mse
+ *     (thresh.cpp:344-385) with the even and odd halves transformed with
+ *     nlevels-1 levels and half level l thresholded by lambda[l] for l in
+ *     [minlevel, min(maxlevel, nlevels-2)].
+ * Synchronous. */
+#define WC_LOSS_SURE 0
+#define WC_LOSS_CV 1
+WC_API int wc_loss_grad(const double* x, int64_t len, int nlevels, int filter, int ttype,
+                        int loss_type, const double* lambda, int minlevel, int maxlevel,
+                        double sigma, double eps, double* loss, double* grad, double* sigma_used,
+                        void* stream);
+
 /* ---- runtime helpers (device memory, pinned host memory, timing) */
 WC_API int wc_device_count(int* count);
 WC_API int wc_malloc_device(void** ptr, size_t bytes);

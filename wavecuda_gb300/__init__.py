@@ -99,6 +99,13 @@ def lib() -> C.CDLL:
     L.wc_modwt_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _vp]
     L.wc_median_mad_device.argtypes = [_vp, C.c_int64, _dp, _dp, _vp]
     L.wc_sequential_sum_device.argtypes = [_vp, C.c_int64, _dp, _vp]
+    L.wc_dwt_adjoint_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        _vp]
+    L.wc_modwt_adjoint_device.argtypes = [_vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_int, _vp]
+    L.wc_soft_threshold_adjoint_device.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, C.c_int,
+                                                   C.c_int, _dp, C.c_int, C.c_int, _vp]
+    L.wc_loss_grad.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
+                               C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _vp]
     L.wc_batch_plan_create.argtypes = [C.POINTER(Signal), C.c_int, C.c_int, C.POINTER(_vp)]
     L.wc_batch_plan_destroy.argtypes = [_vp]
     L.wc_batch_plan_info.argtypes = [_vp, _ip, C.POINTER(C.c_size_t)]
@@ -439,6 +446,32 @@ def median_mad(v) -> tuple:
     check(lib().wc_median_mad_device(buf.ptr, v.size, C.byref(med), C.byref(mad), None))
     buf.free()
     return med.value, mad.value
+
+
+LOSS_SURE, LOSS_CV = 0, 1
+
+
+def loss_grad(x, nlevels, filter, ttype, loss_type, lam, min_level=0, max_level=None,
+              sigma=0.0, eps=0.0):
+    """Loss of per-level soft thresholds and its gradient (wc_loss_grad).
+
+    lam holds one threshold per level (0-based levels); returns
+    (loss, grad, sigma_used)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    if max_level is None:
+        max_level = nlevels - 1
+    grad = np.zeros(nlevels, dtype=np.float64)
+    loss, sig = C.c_double(), C.c_double()
+    buf = DeviceBuffer(x.nbytes)
+    buf.upload(x)
+    try:
+        check(lib().wc_loss_grad(buf.ptr, x.size, nlevels, filter, ttype, loss_type,
+                                 lam.ctypes.data_as(_dp), min_level, max_level, sigma, eps,
+                                 C.byref(loss), grad.ctypes.data_as(_dp), C.byref(sig), None))
+    finally:
+        buf.free()
+    return loss.value, grad, sig.value
 
 
 def sequential_sum(v) -> float:

@@ -65,6 +65,8 @@ enum Slot {
   kSlotConvert,      // FP32 conversions at the boundary
   kSlotStatus,       // device status word
   kSlotBatch,        // batched smoothing (descriptors, results, CTA scratch)
+  kSlotAdjoint,      // loss / gradient evaluation (coefficients, cotangents)
+  kSlotTune,         // batched threshold tuning (coefficients, state)
   kNumSlots
 };
 
