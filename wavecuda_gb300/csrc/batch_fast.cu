@@ -1,0 +1,9 @@
+// Batched smoothing kernel, FP64 data with double-float arithmetic (WC_F64_FAST).
+#include "batch_kernel.cuh"
+
+namespace wc {
+int batch_launch_fast(const BatchArgs& a, int grid, cudaStream_t s) {
+  return batch_launch_p<PDD>(a, grid, s);
+}
+int batch_blocks_per_sm_fast() { return batch_blocks_per_sm_p<PDD>(); }
+}  // namespace wc

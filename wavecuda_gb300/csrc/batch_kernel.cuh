@@ -1,0 +1,824 @@
+#pragma once
+// Batched smoothing kernel: thousands of signals of uneven length, filter, transform
+// and level count in one persistent launch.
+//
+// Each CTA pulls a signal index from a device work queue (atomic counter over
+// a host-sorted order, largest work first) and runs that signal's whole
+// smoothing pipeline -- forward transform, universal or two-fold CV threshold
+// (the reference's CVT, thresh.cpp:203-342, including its device-side
+// golden-section search), final threshold and inverse -- with block-level
+// code, so no host round trip or extra launch happens per signal or per CV
+// iteration.  The pipeline and its quirks are those of smooth.cu; the
+// differences are structural:
+//  * thresholding is fused into the inverse transforms (the coefficient is
+//    thresholded as it is read), so the thresholded copies the reference
+//    builds (y1e->x, y1e->xmod) are never written;
+//  * the MODWT keeps only d_1..d_J and s_J (what the inverse reads);
+//  * log/sqrt constants come from the host's libm (per signal), so the
+//    device's threshold arithmetic reproduces the reference's doubles.
+// A CTA's scratch is a private slice of one workspace allocation, sized for
+// the largest signal of the batch.
+#include <math.h>
+
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
+#include "wc_batch.h"
+#include "wc_common.cuh"
+#include "wc_dd.cuh"
+
+namespace wc {
+namespace {
+
+constexpr int BT = 512;               // threads per CTA
+constexpr uint64_t kFrac = (1ull << 52) - 1;
+
+// ------------------------------------------------------------ values ----
+
+template <class P>
+struct Ops {
+  using T = typename P::T;
+  using V = typename P::V;
+  static __device__ __forceinline__ V load(const T& x) { return P::ld(x); }
+};
+
+template <class P, class S>
+__device__ __forceinline__ typename P::V rd(const S* p, int64_t i) {
+  if constexpr (std::is_same<S, typename P::V>::value) return p[i];
+  else return P::ld(p[i]);
+}
+
+// Threshold in the value domain.  Exact: thresh_coef (thresh.cpp:142-157) in
+// FP64.  FP32: the same in float.  Double-float: |c| < t compared on the
+// normalised pair, soft shrink by a double-float subtraction.
+template <class P>
+struct Th {
+  typename P::V t;
+  int hardness, minl, maxl;
+};
+
+__device__ __forceinline__ double thr(double c, double t, int hard) {
+  if (fabs(c) < t) return 0.0;
+  if (hard == 1) return __dmul_rn((c < 0) ? -1.0 : 1.0, __dsub_rn(fabs(c), t));
+  return c;
+}
+__device__ __forceinline__ float thr(float c, float t, int hard) {
+  if (fabsf(c) < t) return 0.f;
+  if (hard == 1) return ((c < 0) ? -1.f : 1.f) * (fabsf(c) - t);
+  return c;
+}
+__device__ __forceinline__ dd thr(dd c, dd t, int hard) {
+  dd a = c;
+  const bool neg = (c.hi < 0.f) || (c.hi == 0.f && c.lo < 0.f);
+  if (neg) a = {-c.hi, -c.lo};
+  const bool below = (a.hi < t.hi) || (a.hi == t.hi && a.lo < t.lo);
+  if (below) return {0.f, 0.f};
+  if (hard == 1) {
+    dd r = PDD::sub(a, t);
+    return neg ? dd{-r.hi, -r.lo} : r;
+  }
+  return c;
+}
+
+template <class P>
+__device__ __forceinline__ typename P::V thr_v(typename P::V c, const Th<P>& th, int l) {
+  if (l < th.minl || l > th.maxl) return c;
+  return thr(c, th.t, th.hardness);
+}
+
+template <class P>
+__device__ __forceinline__ typename P::V to_v(double x) {
+  if constexpr (std::is_same<typename P::V, dd>::value) return dd_from_double(x);
+  else return (typename P::V)x;
+}
+
+template <class V>
+__device__ __forceinline__ double to_d(V v) {
+  if constexpr (std::is_same<V, dd>::value) return dd_to_double(v);
+  else return (double)v;
+}
+
+// ------------------------------------------------------- DWT (block) ----
+
+// Forward DWT of y (compact, N values, type S) into the interleaved T array
+// `out`; tA/tB hold N/2 values each.
+template <int F, class P, class S>
+__device__ void bdwt_fwd(const S* y, typename P::T* out, int64_t N, int J, typename P::V* tA,
+                         typename P::V* tB) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  int64_t Nl = N;
+  for (int l = 0; l < J; l++) {
+    V* dst = (l & 1) ? tB : tA;
+    const int64_t Pq = Nl >> 1, step = (int64_t)2 << l, off = (int64_t)1 << l;
+    for (int64_t q = threadIdx.x; q < Pq; q += blockDim.x) {
+      V s, d;
+      if constexpr (F == 1) {
+        const V a = (l == 0) ? rd<P>(y, 2 * q) : ((l & 1) ? tA : tB)[2 * q];
+        const V b = (l == 0) ? rd<P>(y, 2 * q + 1) : ((l & 1) ? tA : tB)[2 * q + 1];
+        s = haar_sum<P>(a, b);
+        d = haar_dif<P>(a, b);
+      } else {
+        V v[L];
+#pragma unroll
+        for (int j = 0; j < L; j++) {
+          const int64_t idx = (2 * q + j) & (Nl - 1);
+          v[j] = (l == 0) ? rd<P>(y, idx) : ((l & 1) ? tA : tB)[idx];
+        }
+        typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
+        typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
+#pragma unroll
+        for (int j = 1; j < L; j++) {
+          as = P::acc_add(as, v[j], tap_h(F, j));
+          ad = P::acc_add(ad, v[j], tap_g(F, j));
+        }
+        s = P::acc_fin(as);
+        d = P::acc_fin(ad);
+      }
+      dst[q] = s;
+      out[off + q * step] = P::st(d);
+    }
+    __syncthreads();
+    Nl = Pq;
+  }
+  const typename P::V* src = ((J - 1) & 1) ? tB : tA;
+  for (int64_t q = threadIdx.x; q < Nl; q += blockDim.x) out[q << J] = P::st(src[q]);
+  __syncthreads();
+}
+
+// Inverse DWT of the interleaved coefficients w into `out` (compact, N
+// values, type D), with the details of levels in th's range thresholded as
+// they are read.  The coarse scaling slots q*2^J, q > 0, are read from
+// `coarse` (the reference's stale slots, thresh.cpp:15-35) or from w when
+// coarse == nullptr; slot 0 always from w.
+template <int F, class P, class D>
+__device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_t N, int J,
+                         const Th<P>& th, typename P::V* tA, typename P::V* tB) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  constexpr int H = L / 2;
+  int64_t Nl = N >> J;
+  V* top = ((J - 1) & 1) ? tB : tA;  // level J compact buffer
+  for (int64_t q = threadIdx.x; q < Nl; q += blockDim.x) {
+    if (q == 0 || coarse == nullptr) top[q] = P::ld(w[q << J]);
+    else top[q] = rd<P>(coarse, q << J);
+  }
+  __syncthreads();
+  for (int l = J - 1; l >= 0; l--) {
+    const V* s = (l & 1) ? tB : tA;   // level l+1 values (Nl of them)
+    V* dstv = (l & 1) ? tA : tB;
+    const int64_t off = (int64_t)1 << l, step = (int64_t)2 << l;
+    for (int64_t q = threadIdx.x; q < Nl; q += blockDim.x) {
+      V e, o;
+      if constexpr (F == 1) {
+        const V sv = s[q];
+        const V dv = thr_v<P>(P::ld(w[off + q * step]), th, l);
+        e = haar_sum<P>(sv, dv);
+        o = haar_dif<P>(sv, dv);
+      } else {
+        V sv[H], dv[H];
+#pragma unroll
+        for (int j = 0; j < H; j++) {
+          const int64_t p = (q - j) & (Nl - 1);
+          sv[j] = s[p];
+          dv[j] = thr_v<P>(P::ld(w[off + p * step]), th, l);
+        }
+        typename P::Acc ae = P::acc_init(sv[H - 1], tap_h(F, 2 * (H - 1)));
+        typename P::Acc ao = P::acc_init(sv[H - 1], tap_h(F, 2 * (H - 1) + 1));
+        ae = P::acc_add(ae, dv[H - 1], tap_g(F, 2 * (H - 1)));
+        ao = P::acc_add(ao, dv[H - 1], tap_g(F, 2 * (H - 1) + 1));
+#pragma unroll
+        for (int j = H - 2; j >= 0; j--) {
+          ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+          ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+          ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+          ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+        }
+        e = P::acc_fin(ae);
+        o = P::acc_fin(ao);
+      }
+      if (l == 0) {
+        if constexpr (std::is_same<D, typename P::V>::value) {
+          out[2 * q] = e;
+          out[2 * q + 1] = o;
+        } else {
+          out[2 * q] = P::st(e);
+          out[2 * q + 1] = P::st(o);
+        }
+      } else {
+        dstv[2 * q] = e;
+        dstv[2 * q + 1] = o;
+      }
+    }
+    __syncthreads();
+    Nl <<= 1;
+  }
+}
+
+// ----------------------------------------------------- MODWT (block) ----
+// Stored coefficients: det = [d_1 | ... | d_J] (J blocks of N), sJ (N).
+
+template <int F, class P, class S>
+__device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, int64_t N, int J,
+                           typename P::V* tA, typename P::V* tB) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  for (int l = 0; l < J; l++) {
+    const V* src = (l & 1) ? tA : tB;  // level l values (l >= 1)
+    V* dst = (l & 1) ? tB : tA;
+    const int64_t skip = (int64_t)1 << l;
+    typename P::T* dd_out = det + (int64_t)l * N;
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+      V s, d;
+      if constexpr (F == 1) {
+        const int64_t j = (i + skip) & (N - 1);
+        const V a = (l == 0) ? rd<P>(x, i) : src[i];
+        const V b = (l == 0) ? rd<P>(x, j) : src[j];
+        d = haar_dif<P>(a, b);
+        s = haar_sum<P>(a, b);
+      } else {
+        V v = (l == 0) ? rd<P>(x, i) : src[i];
+        typename P::Acc ad = P::acc_init(v, tap_g(F, 0)), as = P::acc_init(v, tap_h(F, 0));
+#pragma unroll
+        for (int k = 1; k < L; k++) {
+          const int64_t j = (i + (int64_t)k * skip) & (N - 1);
+          v = (l == 0) ? rd<P>(x, j) : src[j];
+          ad = P::acc_add(ad, v, tap_g(F, k));
+          as = P::acc_add(as, v, tap_h(F, k));
+        }
+        d = P::acc_fin(ad);
+        s = P::acc_fin(as);
+      }
+      dd_out[i] = P::st(d);
+      if (l == J - 1) sJ[i] = P::st(s);
+      else dst[i] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <int F, class P, class D>
+__device__ void bmodwt_inv(const typename P::T* det, const typename P::T* sJ, D* out, int64_t N,
+                           int J, const Th<P>& th, typename P::V* tA, typename P::V* tB) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  for (int l = J - 1; l >= 0; l--) {
+    const V* src = ((J - 1 - l) & 1) ? tA : tB;  // s_{l+1} when l < J-1
+    V* dst = ((J - 1 - l) & 1) ? tB : tA;
+    const int64_t skip = (int64_t)1 << l;
+    const typename P::T* dl = det + (int64_t)l * N;
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+      V r;
+      if constexpr (F == 1) {
+        const int64_t j = (i - skip) & (N - 1);
+        const V si = (l == J - 1) ? P::ld(sJ[i]) : src[i];
+        const V sj = (l == J - 1) ? P::ld(sJ[j]) : src[j];
+        V acc = P::add(si, thr_v<P>(P::ld(dl[i]), th, l));
+        acc = P::add(acc, sj);
+        acc = P::sub(acc, thr_v<P>(P::ld(dl[j]), th, l));
+        r = P::mul(acc, kHInvR2);
+      } else {
+        typename P::Acc acc;
+#pragma unroll
+        for (int t = 0; t < L; t++) {
+          const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
+          const int64_t j = (i - (int64_t)k * skip) & (N - 1);
+          const V sv = (l == J - 1) ? P::ld(sJ[j]) : src[j];
+          const V dv = thr_v<P>(P::ld(dl[j]), th, l);
+          if (t == 0) acc = P::acc_init(sv, tap_h(F, k));
+          else acc = P::acc_add(acc, sv, tap_h(F, k));
+          acc = P::acc_add(acc, dv, tap_g(F, k));
+        }
+        r = P::half(P::acc_fin(acc));
+      }
+      if (l == 0) {
+        if constexpr (std::is_same<D, V>::value) out[i] = r;
+        else out[i] = P::st(r);
+      } else {
+        dst[i] = r;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------- radix select (block) --
+
+__device__ __forceinline__ uint64_t key_of(double v) {
+  uint64_t u = (uint64_t)__double_as_longlong(v);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double val_of(uint64_t k) {
+  uint64_t u = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// Source of the universal threshold's values: `nseg` segments of `seg_len`
+// values `seg_stride` apart, or (dwt_J > 0) the DWT details i in [1, len)
+// with level ctz(i) in [minl, maxl].
+template <class T>
+struct Src {
+  const T* base;
+  int64_t seg_len, seg_stride, nseg;
+  int dwt_J, minl, maxl;
+  int64_t count;
+};
+
+struct SelShared {
+  unsigned int h[2][256];
+  uint64_t prefix[2], mask[2];
+  long long rank[2];
+};
+
+template <class T, class Fn>
+__device__ __forceinline__ void for_each_src(const Src<T>& s, Fn fn) {
+  if (s.dwt_J > 0) {
+    const int64_t len = s.seg_len;
+    for (int64_t i = 1 + threadIdx.x; i < len; i += blockDim.x) {
+      const int l = __ffsll((long long)i) - 1;
+      if (l >= s.dwt_J || l < s.minl || l > s.maxl) continue;
+      fn((double)s.base[i]);
+    }
+  } else {
+    const int64_t total = s.seg_len * s.nseg;
+    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const int64_t seg = e / s.seg_len, off = e - seg * s.seg_len;
+      fn((double)s.base[seg * s.seg_stride + off]);
+    }
+  }
+}
+
+// Values of ranks ka and kb (0-based) of the source, into *va, *vb (valid in
+// every thread on return).
+template <class T>
+__device__ void bselect(const Src<T>& src, long long ka, long long kb, SelShared& sh, double* va,
+                        double* vb) {
+  if (threadIdx.x == 0) {
+    sh.prefix[0] = sh.prefix[1] = 0;
+    sh.mask[0] = sh.mask[1] = 0;
+    sh.rank[0] = ka;
+    sh.rank[1] = kb;
+  }
+  __syncthreads();
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&sh.h[0][0])[i] = 0;
+    __syncthreads();
+    const uint64_t p0 = sh.prefix[0], p1 = sh.prefix[1], m0 = sh.mask[0], m1 = sh.mask[1];
+    for_each_src(src, [&](double v) {
+      const uint64_t k = key_of(v);
+      const int d = (int)((k >> shift) & 255);
+      if ((k & m0) == p0) atomicAdd(&sh.h[0][d], 1u);
+      if ((k & m1) == p1) atomicAdd(&sh.h[1][d], 1u);
+    });
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const int r = threadIdx.x;
+      unsigned long long cum = 0;
+      int d = 0;
+      for (; d < 255; d++) {
+        if ((unsigned long long)sh.rank[r] < cum + sh.h[r][d]) break;
+        cum += sh.h[r][d];
+      }
+      sh.rank[r] -= (long long)cum;
+      sh.prefix[r] |= (uint64_t)d << shift;
+      sh.mask[r] |= (uint64_t)255 << shift;
+    }
+    __syncthreads();
+  }
+  *va = val_of(sh.prefix[0]);
+  *vb = val_of(sh.prefix[1]);
+  __syncthreads();
+}
+
+// median / mad of the source (utils.cpp:166-203); dev_buf holds count doubles.
+template <class T>
+__device__ void bmedian_mad(const Src<T>& src, double* dev_buf, SelShared& sh, double* med,
+                            double* mad) {
+  const long long n = src.count;
+  double a, b;
+  bselect(src, (n - 1) / 2, n / 2, sh, &a, &b);
+  const double m = __dmul_rn(0.5, __dadd_rn(a, b));
+  // |x - med| compactly (order irrelevant to the median)
+  __shared__ unsigned long long pos;
+  if (threadIdx.x == 0) pos = 0;
+  __syncthreads();
+  for_each_src(src, [&](double v) {
+    const unsigned long long k = atomicAdd(&pos, 1ull);
+    dev_buf[k] = fabs(__dsub_rn(v, m));
+  });
+  __syncthreads();
+  Src<double> ds{dev_buf, n, n, 1, 0, 0, 0, n};
+  bselect(ds, (n - 1) / 2, n / 2, sh, &a, &b);
+  *med = m;
+  *mad = __dmul_rn(1.4826, __dmul_rn(0.5, __dadd_rn(a, b)));
+}
+
+// -------------------------------------------------- exact loss sum (block) --
+// Same replay as cv_sum.cu with chunks of blockDim terms.
+
+__device__ __forceinline__ void q_of(double v, int eb_m, long long& q, bool& bad) {
+  const uint64_t vb = (uint64_t)__double_as_longlong(v);
+  const int ebv = (int)((vb >> 52) & 0x7FF);
+  q = 0;
+  bad = false;
+  if (eb_m <= 0 || eb_m >= 0x7FF || ebv == 0x7FF || ebv >= eb_m) {
+    bad = true;
+    return;
+  }
+  const uint64_t M = (vb & kFrac) | (ebv ? (1ull << 52) : 0ull);
+  if (M == 0) return;
+  const int s = eb_m - (ebv ? ebv : 1);
+  if (s == 0) {
+    q = (long long)M;
+    return;
+  }
+  if (s > 63) return;
+  const uint64_t rem = M & ((1ull << s) - 1), half = 1ull << (s - 1);
+  if (rem == half) {
+    bad = true;
+    return;
+  }
+  q = (long long)((M >> s) + (rem > half ? 1 : 0));
+}
+
+struct SumShared {
+  long long warp_tot[32];
+  unsigned long long mb;
+  long long add;
+  int kstar;
+};
+
+__device__ __forceinline__ long long bscan_incl(long long x, SumShared& sh) {
+  const int l = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (l >= o) x += y;
+  }
+  if (l == 31) sh.warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    long long t = (l < nw) ? sh.warp_tot[l] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, t, o);
+      if (l >= o) t += y;
+    }
+    if (l < nw) sh.warp_tot[l] = t;
+  }
+  __syncthreads();
+  const long long r = x + (w > 0 ? sh.warp_tot[w - 1] : 0);
+  __syncthreads();
+  return r;
+}
+
+// Serial-order FP64 sum of v[0..n) (all >= 0); result in every thread.
+// Chunks are blockDim terms; each chunk is added with one integer add when
+// the whole chunk stays in m's binade with no tie, else replayed with a
+// block prefix sum up to the first crossing / tie.
+__device__ double bseq_sum(const double* v, int64_t n, SumShared& sh) {
+  const int B = blockDim.x;
+  if (threadIdx.x == 0) sh.mb = 0ull;
+  __syncthreads();
+  for (int64_t base = 0; base < n; base += B) {
+    const int len = (int)((n - base < B) ? (n - base) : B);
+    const double myv = (threadIdx.x < len) ? v[base + threadIdx.x] : 0.0;
+    int pos = 0;
+    while (pos < len) {
+      const unsigned long long mb = sh.mb;
+      long long q = 0;
+      bool bad = false;
+      const bool active = threadIdx.x >= pos && threadIdx.x < len;
+      if (active) q_of(myv, (int)(mb >> 52), q, bad);
+      if (!active || bad) q = 0;
+      const long long incl = bscan_incl(q, sh);
+      const bool stop = active && (bad || (mb & kFrac) + (unsigned long long)incl >= (1ull << 52));
+      if (threadIdx.x == 0) sh.kstar = len;
+      __syncthreads();
+      if (stop) atomicMin(&sh.kstar, (int)threadIdx.x);
+      __syncthreads();
+      const int kstar = sh.kstar;
+      if (kstar == len) {
+        if ((int)threadIdx.x == len - 1) sh.add = incl;
+      } else if ((int)threadIdx.x == kstar) {
+        sh.add = incl - q;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long m2 = sh.mb + (unsigned long long)sh.add;
+        if (kstar < len)
+          m2 = (unsigned long long)__double_as_longlong(
+              __dadd_rn(__longlong_as_double((long long)m2), v[base + kstar]));
+        sh.mb = m2;
+      }
+      __syncthreads();
+      pos = kstar + 1;
+    }
+  }
+  const double m = __longlong_as_double((long long)sh.mb);
+  __syncthreads();
+  return m;
+}
+
+// ------------------------------------------------------ CV loss (block) --
+
+template <class Y>
+__device__ void bcv_terms(const Y* ye, const Y* yo, const double* xn, int64_t lenh,
+                          double* terms) {
+  for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
+    double yie, yio;
+    if (j == 0) {
+      yie = to_d(yo[0]);
+      yio = __dmul_rn(0.5, __dadd_rn(to_d(ye[0]), to_d(ye[1])));
+    } else if (j == lenh - 1) {
+      yio = to_d(ye[lenh - 1]);
+      yie = __dmul_rn(0.5, __dadd_rn(to_d(yo[j]), to_d(yo[j - 1])));
+    } else {
+      yio = __dmul_rn(0.5, __dadd_rn(to_d(ye[j]), to_d(ye[j + 1])));
+      yie = __dmul_rn(0.5, __dadd_rn(to_d(yo[j]), to_d(yo[j - 1])));
+    }
+    const double a = __dsub_rn(yie, xn[2 * j]);
+    const double b = __dsub_rn(yio, xn[2 * j + 1]);
+    terms[j] = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------ pipeline --
+
+struct CtaScratch {
+  char* base;
+  size_t off;
+  template <class T>
+  __device__ T* take(int64_t n) {
+    T* p = reinterpret_cast<T*>(base + off);
+    off += ((sizeof(T) * (size_t)n + 255) / 256) * 256;
+    return p;
+  }
+};
+
+struct PipeShared {
+  SelShared sel;
+  SumShared sum;
+};
+
+// Forward transform of a compact signal s (length n) into the coefficient
+// store: DWT -> w (interleaved, n); MODWT -> det (J*n) and sJ (n).
+template <int F, class P, class S>
+__device__ void fwd_any(int ttype, const S* s, typename P::T* w, typename P::T* sJ, int64_t n,
+                        int J, typename P::V* tA, typename P::V* tB) {
+  if (ttype == 0) bdwt_fwd<F, P, S>(s, w, n, J, tA, tB);
+  else bmodwt_fwd<F, P, S>(s, w, sJ, n, J, tA, tB);
+}
+
+template <int F, class P, class D>
+__device__ void inv_any(int ttype, const typename P::T* w, const typename P::T* sJ,
+                        const D* coarse, D* out, int64_t n, int J, const Th<P>& th,
+                        typename P::V* tA, typename P::V* tB) {
+  if (ttype == 0) bdwt_inv<F, P, D>(w, coarse, out, n, J, th, tA, tB);
+  else bmodwt_inv<F, P, D>(w, sJ, out, n, J, th, tA, tB);
+}
+
+// univ_thresh (thresh.cpp:170-201) on the stored coefficients.
+template <class T>
+__device__ double buniv(int ttype, const T* w, int64_t n, int J, int minl, int maxl,
+                        double sq_nm1, double sq_n, double* devbuf, PipeShared& sh) {
+  Src<T> src;
+  double scale;
+  if (ttype == 0) {
+    if (minl == 0 && maxl == J - 1) {
+      src = Src<T>{w + 1, n - 1, n - 1, 1, 0, 0, 0, n - 1};
+      scale = sq_nm1;
+    } else {
+      int64_t cnt = 0;
+      for (int l = minl; l <= maxl; l++) cnt += n >> (l + 1);
+      src = Src<T>{w, n, n, 1, J, minl, maxl, cnt};
+      scale = sq_n;
+    }
+  } else {
+    const int64_t nb = maxl - minl + 1;  // blocks 0 .. maxl-minl (wavutils.cpp:716-722)
+    src = Src<T>{w, n, n, nb, 0, 0, 0, nb * n};
+    scale = sq_n;
+  }
+  double med, mad;
+  bmedian_mad(src, devbuf, sh.sel, &med, &mad);
+  return __dmul_rn(mad, scale);
+}
+
+__device__ __forceinline__ bool range_ok(int64_t n, int J, int minl, int maxl, int L) {
+  int maxlev = 0;
+  while (((int64_t)L << maxlev) <= n) maxlev++;
+  if (J < 1 || J > maxlev || minl < 0 || maxl < 0) return false;
+  return minl <= maxl && maxl < J;
+}
+
+template <int F, class P>
+__device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch cs, PipeShared& sh) {
+  using T = typename P::T;
+  using V = typename P::V;
+  const BatchDesc d = a.desc[idx];
+  BatchResult* res = a.res + idx;
+  double* x = a.data + d.off;
+  const int64_t n = d.n, lenh = n / 2;
+  const int J = d.J, tt = d.ttype, L = filter_len(F);
+  const bool mod = (tt == 1);
+
+  // x in the working precision
+  T* xt = cs.take<T>(n);
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) xt[i] = (T)x[i];
+  T* w = cs.take<T>(mod ? (int64_t)J * n : n);
+  T* wsJ = cs.take<T>(mod ? n : 1);
+  V* tA = cs.take<V>(n);
+  V* tB = cs.take<V>(n);
+  double* devbuf = cs.take<double>(mod ? (int64_t)J * n : n);
+  __syncthreads();
+
+  double t = d.thresh, t_univ = 0.0, min_margin = 1e300;
+  int iters = 0;
+  fwd_any<F, P, T>(tt, xt, w, wsJ, n, J, tA, tB);
+
+  if (d.threshtype == 2) {
+    if (!range_ok(n, J, d.minl, d.maxl, L) || J <= 1) {
+      if (threadIdx.x == 0) {
+        res->thresh = 0.0;
+        res->iterations = 0;
+        res->status = 0;
+        res->thresh_univ = 0.0;
+        res->kept = res->zeroed = 0;
+        res->min_margin = 0.0;
+      }
+      return;  // thresh.cpp:223-231: x untouched
+    }
+    const int lv1 = J - 1;
+    const int maxl1 = d.maxl - 1;
+    t_univ = buniv<T>(tt, w, n, J, d.minl, d.maxl, d.sq_nm1, d.sq_n, devbuf, sh);
+    // half-length vectors: coefficient stores and the four work vectors
+    T* we = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
+    T* weJ = cs.take<T>(mod ? lenh : 1);
+    T* wo = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
+    T* woJ = cs.take<T>(mod ? lenh : 1);
+    V* y[4];
+    for (int k = 0; k < 4; k++) y[k] = cs.take<V>(lenh);
+    double* terms = cs.take<double>(lenh);
+    for (int64_t i = threadIdx.x; i < 4 * lenh; i += blockDim.x) {
+      // zero the work vectors (fresh zero-filled pages in the reference)
+      (y[i / lenh])[i % lenh] = to_v<P>(0.0);
+    }
+    for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
+      reinterpret_cast<T*>(tA)[j] = (T)x[2 * j];
+      reinterpret_cast<T*>(tB)[j] = (T)x[2 * j + 1];
+    }
+    __syncthreads();
+    // even/odd halves live in tA/tB's first halves as T; transform them
+    // with the upper halves of tA/tB as level buffers
+    {
+      T* ev = reinterpret_cast<T*>(tA);
+      T* od = reinterpret_cast<T*>(tB);
+      V* uA = tA + lenh;
+      V* uB = tB + lenh;
+      // forward of the even half uses uA/uB for levels; copy odd half first
+      // into devbuf so both fit.
+      T* od2 = reinterpret_cast<T*>(devbuf);
+      for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) od2[j] = od[j];
+      __syncthreads();
+      fwd_any<F, P, T>(tt, ev, we, weJ, lenh, lv1, uA, uB);
+      fwd_any<F, P, T>(tt, od2, wo, woJ, lenh, lv1, uA, uB);
+    }
+    const bool half_ok = range_ok(lenh, lv1, d.minl, maxl1, L);
+    auto step = [&](int k, double tk) {
+      // threshold(we|wo, y_k, tk) then transform(y_k, BWD)
+      if (!half_ok) return;  // never thresholded: y_k stays zero
+      Th<P> th{to_v<P>(tk), d.hardness, d.minl, maxl1};
+      const bool even = (k & 1) == 0;
+      const T* ws = even ? we : wo;
+      const T* wJ = even ? weJ : woJ;
+      // DWT: coarse slots k*2^(J-1), k>0, come from y's previous content
+      inv_any<F, P, V>(tt, ws, wJ, (tt == 0) ? y[k] : nullptr, y[k], lenh, lv1, th, tA, tB);
+    };
+    const double R = 0.61803399, C = __dsub_rn(1.0, R);
+    double ta = 0., tc = t_univ;
+    double tb = __dmul_rn(tc, 0.5);
+    double t0 = ta, t2 = tb, t1 = __dsub_rn(tb, __dmul_rn(C, __dsub_rn(tb, ta))), t3 = tc;
+    step(0, t1);
+    step(1, t1);
+    step(2, t2);
+    step(3, t2);
+    bcv_terms<V>(y[0], y[1], x, lenh, terms);
+    double m1 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+    bcv_terms<V>(y[2], y[3], x, lenh, terms);
+    double m2 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+    while (fabs(__dsub_rn(t3, t0)) > __dmul_rn(d.tol, __dadd_rn(t1, t2))) {
+      if (iters > 50) break;
+      if (m1 != 0.0) min_margin = fmin(min_margin, fabs(__dsub_rn(m1, m2)) / fabs(m1));
+      if (m2 < m1) {
+        t0 = t1; t1 = t2; t2 = __dadd_rn(__dmul_rn(R, t2), __dmul_rn(C, t3));
+        m1 = m2;
+        step(2, t2);
+        step(3, t2);
+        bcv_terms<V>(y[2], y[3], x, lenh, terms);
+        m2 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+      } else {
+        t3 = t2; t2 = t1; t1 = __dadd_rn(__dmul_rn(R, t1), __dmul_rn(C, t0));
+        m2 = m1;
+        step(0, t1);
+        step(1, t1);
+        bcv_terms<V>(y[0], y[1], x, lenh, terms);
+        m1 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+      }
+      iters++;
+    }
+    t = m1 < m2 ? t1 : t2;
+    t = __ddiv_rn(t, d.rescale);
+  } else if (d.threshtype == 1) {
+    t_univ = buniv<T>(tt, w, n, J, 0, 0, d.sq_nm1, d.sq_n, devbuf, sh);
+    t = t_univ;
+  }
+
+  // kept / zeroed over [minl, maxl] on the unthresholded coefficients
+  long long kept = 0, zeroed = 0;
+  const bool ok = range_ok(n, J, d.minl, d.maxl, L);
+  if (ok) {
+    __shared__ unsigned long long cnt[2];
+    if (threadIdx.x == 0) cnt[0] = cnt[1] = 0;
+    __syncthreads();
+    unsigned long long k0 = 0, z0 = 0;
+    if (!mod) {
+      for (int64_t i = 1 + threadIdx.x; i < n; i += blockDim.x) {
+        const int l = __ffsll((long long)i) - 1;
+        if (l >= J || l < d.minl || l > d.maxl) continue;
+        if (fabs((double)w[i]) < t) z0++; else k0++;
+      }
+    } else {
+      for (int64_t e = threadIdx.x; e < (int64_t)(d.maxl - d.minl + 1) * n; e += blockDim.x) {
+        if (fabs((double)w[(int64_t)d.minl * n + e]) < t) z0++; else k0++;
+      }
+    }
+    atomicAdd(&cnt[0], k0);
+    atomicAdd(&cnt[1], z0);
+    __syncthreads();
+    kept = (long long)cnt[0];
+    zeroed = (long long)cnt[1];
+  }
+  // final threshold + inverse straight into x (FP64 out)
+  Th<P> th{to_v<P>(t), d.hardness, ok ? d.minl : 1 << 30, ok ? d.maxl : -1};
+  if constexpr (std::is_same<T, double>::value) {
+    inv_any<F, P, double>(tt, w, wsJ, nullptr, x, n, J, th, tA, tB);
+  } else {
+    inv_any<F, P, T>(tt, w, wsJ, nullptr, xt, n, J, th, tA, tB);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = (double)xt[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    res->thresh = t;
+    res->thresh_univ = t_univ;
+    res->iterations = iters;
+    res->status = 0;
+    res->kept = kept;
+    res->zeroed = zeroed;
+    res->min_margin = (d.threshtype == 2) ? min_margin : 0.0;
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(BT) smooth_batch_kernel(BatchArgs a) {
+  __shared__ PipeShared sh;
+  __shared__ int s_sig;
+  CtaScratch cs{a.scratch + (size_t)blockIdx.x * a.scratch_per_cta, 0};
+  while (true) {
+    if (threadIdx.x == 0) s_sig = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int k = s_sig;
+    __syncthreads();
+    if (k >= a.nsig) break;
+    const int idx = a.order[k];
+    cs.off = 0;
+    switch (a.desc[idx].F) {
+      case 1: smooth_one<1, P>(a, idx, cs, sh); break;
+      case 2: smooth_one<2, P>(a, idx, cs, sh); break;
+      case 3: smooth_one<3, P>(a, idx, cs, sh); break;
+      case 4: smooth_one<4, P>(a, idx, cs, sh); break;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// One precision's launch and occupancy query.  Each precision is compiled in
+// its own translation unit (batch_exact.cu, batch_fast.cu, batch_f32.cu) so
+// the three instantiations of the pipeline build in parallel.
+template <class P>
+int batch_launch_p(const BatchArgs& a, int grid, cudaStream_t s) {
+  smooth_batch_kernel<P><<<grid, BT, 0, s>>>(a);
+  return after_launch("smooth_batch_kernel");
+}
+
+template <class P>
+int batch_blocks_per_sm_p() {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, smooth_batch_kernel<P>, BT, 0) !=
+      cudaSuccess)
+    return 1;
+  return per < 1 ? 1 : per;
+}
+
+}  // namespace wc

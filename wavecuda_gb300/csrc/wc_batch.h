@@ -1,4 +1,4 @@
-// Batched smoothing: descriptors shared by the persistent kernel (batch.cu)
+// Batched smoothing: descriptors shared by the persistent kernel (batch_kernel.cuh)
 // and its host-side plan (batch_plan.cu).
 #pragma once
 
@@ -36,5 +36,14 @@ struct BatchArgs {
 size_t batch_scratch_bytes(const BatchDesc& d, int prec);
 int batch_launch(const BatchArgs& a, int prec, int grid, cudaStream_t s);
 int batch_max_ctas(int prec);
+
+// Per-precision instantiations of the persistent kernel (batch_exact.cu,
+// batch_fast.cu, batch_f32.cu): launch, and resident CTAs per SM.
+int batch_launch_exact(const BatchArgs& a, int grid, cudaStream_t s);
+int batch_launch_fast(const BatchArgs& a, int grid, cudaStream_t s);
+int batch_launch_f32(const BatchArgs& a, int grid, cudaStream_t s);
+int batch_blocks_per_sm_exact();
+int batch_blocks_per_sm_fast();
+int batch_blocks_per_sm_f32();
 
 }  // namespace wc
