@@ -140,17 +140,24 @@ class Dist:
 
 # ---------------------------------------------------------------- CPU arm --
 
-def cpu_time_dwt(n: int, filt: int, J: int, budget_s: float, use_ref: bool):
-    """Times fwd+inv DWT on the CPU (oracle port, or the reference's own
-    compiled sources when available) until budget_s has elapsed."""
+def cpu_impl(use_ref: bool):
+    """The CPU arm: the reference's own compiled sources (serial, as the
+    reference dispatches them) when they were built here, else the oracle
+    port with its level loops on every host core (bit-identical results).
+    Returns (impl, kind, threads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     if not os.path.exists(pyoracle.ORACLE_SO):
         pyoracle.build()
     if use_ref and pyoracle.reference_available():
-        impl, kind = pyoracle.Reference(), "reference"
-    else:
-        impl, kind = pyoracle.Oracle(), "port"
+        return pyoracle.Reference(), "reference", 1
+    impl = pyoracle.Oracle()
+    return impl, "port", impl.set_threads(0)
+
+
+def cpu_time_dwt(n: int, filt: int, J: int, budget_s: float, use_ref: bool):
+    """Times fwd+inv DWT on the CPU until budget_s has elapsed."""
+    impl, kind, threads = cpu_impl(use_ref)
     from wavecuda_gb300 import signals
     x = signals.roofline_input(n, seed=1)
     reps, t_total = 0, 0.0
@@ -160,7 +167,7 @@ def cpu_time_dwt(n: int, filt: int, J: int, budget_s: float, use_ref: bool):
         impl.dwt(w, J, filt, 0)
         t_total += time.perf_counter() - t0
         reps += 1
-    return reps * n / t_total / 1e9, kind, reps, t_total
+    return reps * n / t_total / 1e9, kind, reps, t_total, threads
 
 
 # ---------------------------------------------------------------- GPU arm --
@@ -339,9 +346,10 @@ def ours(args):
            "pr_err": pr_err}
 
     if dist.rank == 0 and not args.no_cpu:
-        v, kind, reps, tt = cpu_time_dwt(1 << args.cpu_log2n, filt, min(J, args.cpu_log2n - 2),
-                                         args.cpu_budget, use_ref=False)
-        out["cpu_baseline"] = {"value": v, "unit": "Gsamples/s", "cores": 1, "kind": kind,
+        v, kind, reps, tt, threads = cpu_time_dwt(1 << args.cpu_log2n, filt,
+                                                  min(J, args.cpu_log2n - 2), args.cpu_budget,
+                                                  use_ref=False)
+        out["cpu_baseline"] = {"value": v, "unit": "Gsamples/s", "cores": threads, "kind": kind,
                                "sample": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.cpu_log2n}, "
                                          f"{reps} reps, {tt:.1f} s"}
 
@@ -469,13 +477,7 @@ def reference(args):
     n = 1 << args.log2n
     filt, J = args.filter, args.levels
     # each step: one fwd+inv of the full n = 2^26 workload on the host
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    if not os.path.exists(pyoracle.ORACLE_SO):
-        pyoracle.build()
-    use_ref = pyoracle.reference_available()
-    impl = pyoracle.Reference() if use_ref else pyoracle.Oracle()
-    kind = "reference" if use_ref else "port"
+    impl, kind, threads = cpu_impl(use_ref=True)
     from wavecuda_gb300 import signals
     x = signals.roofline_input(n, seed=1)
     for _ in range(args.warmup):
@@ -491,31 +493,38 @@ def reference(args):
            "data": "synthetic: iid N(0,1) + 8 sinusoids, seeded", "impl": "reference",
            "config": {"workload": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.log2n}, J={J}, FP64",
                       "n": n, "levels": J, "filter": FILTERS[filt]},
-           "cpu_baseline": {"value": v, "unit": "Gsamples/s", "cores": 1, "kind": kind,
-                            "sample": f"full workload, {args.steps} steps; the reference's "
-                                      "dispatched CPU transform is serial"},
+           "cpu_baseline": {"value": v, "unit": "Gsamples/s", "cores": threads, "kind": kind,
+                            "sample": f"full workload, {args.steps} steps"
+                                      + ("; the reference's dispatched CPU transform is serial"
+                                         if kind == "reference" else
+                                         "; oracle port, level loops on every host core")},
            "e2e": {"value": v, "unit": "Gsamples/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
 def profile_case(args):
-    """Runs one small single-kernel case twice (for ncu captures)."""
+    """Runs one small case twice (for ncu captures): forward then inverse of
+    a 2^log2n signal, DWT with J = min(16, log2n - 2) or MODWT with J = 4."""
     import wavecuda_gb300 as wc
     n = 1 << args.log2n
     x = np.random.default_rng(0).standard_normal(n)
     L = wc.lib()
-    a, b = wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n * 2 * 4)
-    a.upload(x)
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
+    es = 4 if prec == 2 else 8
+    a, b, r = wc.DeviceBuffer(es * n), wc.DeviceBuffer(es * n * 2 * 4), wc.DeviceBuffer(es * n)
+    a.upload(x.astype(np.float32) if prec == 2 else x)
     if args.tiling:
         wc.set_dwt_tiling(filt, prec, *[int(v) for v in args.tiling.split(":")])
     for _ in range(2):
         if kind == "dwt":
-            wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, min(16, args.log2n - 2), filt, prec, None))
+            J = min(16, args.log2n - 2)
+            wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, J, filt, prec, None))
+            wc.check(L.wc_dwt_device(b.ptr, r.ptr, n, 0, J, filt, prec, None))
         else:
             wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 1, 4, filt, prec, None))
+            wc.check(L.wc_modwt_device(r.ptr, b.ptr, n, 0, 4, filt, prec, None))
         wc.check(L.wc_stream_synchronize(None))
     print("ok", args.profile_case)
 

@@ -89,6 +89,14 @@ class Oracle:
                                 C.c_int, C.c_int, C.c_int, C.c_double]
         L.wo_count_kept.argtypes = [_dp, _dp, _i64, C.c_int, C.c_int, C.c_double,
                                     C.c_int, C.c_int, C.POINTER(_i64), C.POINTER(_i64)]
+        L.wo_set_threads.argtypes = [C.c_int]
+        L.wo_get_threads.restype = C.c_int
+
+    def set_threads(self, n: int) -> int:
+        """Threads of the transform loops (n <= 0: every core); returns the
+        count in effect.  Results do not depend on it."""
+        self.lib.wo_set_threads(n)
+        return self.lib.wo_get_threads()
 
     def levels(self, n, nlevels, filt):
         return self.lib.wo_check_len_levels(n, nlevels, FILTER_LEN[filt])

@@ -12,10 +12,17 @@
  * the reference expressions cited at each function.  Subtractions of a
  * product in the reference (a - x*C) are written as additions of x*(-C),
  * which rounds identically.  Indices are 64-bit.
+ *
+ * The per-level transform loops run on OpenMP threads for long levels.  Each
+ * output of a level depends only on the previous level, so the thread count
+ * changes no result; wo_set_threads(1) gives the reference's serial loop.
  */
 #include "wavoracle.h"
 
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -72,6 +79,25 @@ static int get_taps(int filter, double* h, double* g) {
   return L;
 }
 
+/* Levels shorter than this run serially. */
+#define WO_PAR_MIN 32768
+
+void wo_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n > 0 ? n : omp_get_num_procs());
+#else
+  (void)n;
+#endif
+}
+
+int wo_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
 static int is_pow2(int64_t n) { return n > 0 && (n & (n - 1)) == 0; }
 
 /* wavutils.cpp:48-64 */
@@ -101,8 +127,10 @@ static int check_levels_range(int64_t len, int nlevels, int minlevel,
 static void dwt_fwd_level(double* x, int64_t len, int64_t skip, int filter,
                           double* tmp) {
   const int64_t N = len / skip;
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
   for (int64_t m = 0; m < N; m++) tmp[m] = x[m * skip];
   if (filter == WO_HAAR) {
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
     for (int64_t q = 0; q < N / 2; q++) {
       double a = tmp[2 * q], b = tmp[2 * q + 1];
       x[(2 * q + 1) * skip] = (a - b) * kInvR2;
@@ -112,6 +140,7 @@ static void dwt_fwd_level(double* x, int64_t len, int64_t skip, int filter,
   }
   double h[8], g[8];
   int L = get_taps(filter, h, g);
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
   for (int64_t q = 0; q < N / 2; q++) {
     double s = tmp[(2 * q) % N] * h[0];
     double d = tmp[(2 * q) % N] * g[0];
@@ -131,8 +160,10 @@ static void dwt_fwd_level(double* x, int64_t len, int64_t skip, int filter,
 static void dwt_inv_level(double* x, int64_t len, int64_t skip, int filter,
                           double* tmp) {
   const int64_t N = len / skip, P = N / 2;
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
   for (int64_t m = 0; m < N; m++) tmp[m] = x[m * skip];
   if (filter == WO_HAAR) {
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
     for (int64_t q = 0; q < P; q++) {
       double a = tmp[2 * q], b = tmp[2 * q + 1];
       x[(2 * q + 1) * skip] = (a - b) * kInvR2;
@@ -143,6 +174,7 @@ static void dwt_inv_level(double* x, int64_t len, int64_t skip, int filter,
   double h[8], g[8];
   int L = get_taps(filter, h, g);
   const int H = L / 2;
+#pragma omp parallel for if (N >= WO_PAR_MIN) schedule(static)
   for (int64_t q = 0; q < P; q++) {
     double e = 0.0, o = 0.0;
     for (int j = H - 1; j >= 0; j--) {
@@ -190,6 +222,7 @@ static void modwt_fwd_level(const double* X, double* S, double* D, int64_t len,
                             int64_t skip, int filter) {
   const int64_t mask = len - 1;
   if (filter == WO_HAAR) {
+#pragma omp parallel for if (len >= WO_PAR_MIN) schedule(static)
     for (int64_t i = 0; i < len; i++) {
       double a = X[i], b = X[(i + skip) & mask];
       D[i] = (a - b) * kInvR2;
@@ -199,6 +232,7 @@ static void modwt_fwd_level(const double* X, double* S, double* D, int64_t len,
   }
   double h[8], g[8];
   int L = get_taps(filter, h, g);
+#pragma omp parallel for if (len >= WO_PAR_MIN) schedule(static)
   for (int64_t i = 0; i < len; i++) {
     double v = X[i];
     double d = v * g[0], s = v * h[0];
@@ -219,6 +253,7 @@ static void modwt_inv_level(double* Xout, const double* S, const double* D,
                             int64_t len, int64_t skip, int filter) {
   const int64_t mask = len - 1;
   if (filter == WO_HAAR) {
+#pragma omp parallel for if (len >= WO_PAR_MIN) schedule(static)
     for (int64_t i = 0; i < len; i++) {
       int64_t j = (i - skip) & mask;
       Xout[i] = (S[i] + D[i] + S[j] - D[j]) * kHInvR2;
@@ -230,6 +265,7 @@ static void modwt_inv_level(double* Xout, const double* S, const double* D,
   int order[8], n = 0;
   for (int k = L - 2; k >= 0; k -= 2) order[n++] = k;
   for (int k = L - 1; k >= 1; k -= 2) order[n++] = k;
+#pragma omp parallel for if (len >= WO_PAR_MIN) schedule(static)
   for (int64_t i = 0; i < len; i++) {
     double acc = 0.0;
     for (int t = 0; t < L; t++) {

@@ -30,6 +30,11 @@ int wo_filter_length(int filter);
 /* check_len_levels (wavutils.cpp:48-64): 0 on error, else the level count. */
 int wo_check_len_levels(int64_t len, int nlevels, int filterlen);
 
+/* Threads of the per-level transform loops (n <= 0: every core).  Results do
+ * not depend on it. */
+void wo_set_threads(int n);
+int wo_get_threads(void);
+
 /* DWT, interleaved in place (haar.cpp:9-30). */
 int wo_dwt(double* x, int64_t len, int sense, int nlevels, int filter);
 
