@@ -380,6 +380,8 @@ def ours(args):
         out["tiling"] = tiling
     if not args.no_batch:
         out["batched"] = batch_bench(wc, args)
+    if not args.no_fit:
+        out["tuned"] = fit_bench(wc, args)
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -470,6 +472,71 @@ def batch_bench(wc, args):
     return out
 
 
+def fit_bench(wc, args):
+    """Gradient-tuned per-level thresholds against the plain golden-section CV
+    smoothing: 256 signals of n = 2^16 (shapes doppler/blocks/bumps/heavisine
+    alike at SNR 3 and 7), MODWT LA8 with 10 levels, soft thresholds, SURE and
+    CV losses, 60 Adam steps, one persistent launch per batch."""
+    import ctypes as C
+    from wavecuda_gb300 import signals as sg
+    L = wc.lib()
+    n, nsig, J = 1 << 16, args.fit_signals, 10
+    shapes = list(sg.SHAPES)
+    clean = np.stack([sg.SHAPES[shapes[i % 4]](n, i) for i in range(nsig)])
+    X = np.stack([sg.noisy(clean[i], (3.0, 7.0)[(i // 4) % 2], seed=7000 + i)
+                  for i in range(nsig)])
+    out = {"workload": f"{nsig} signals, n = 2^16, MODWT LA8, J = 10, soft, per-level "
+                       "thresholds by 60 Adam steps on the loss through the adjoint kernels",
+           "iterations": 60}
+    rng = np.random.default_rng(9)
+    sub = sorted(rng.choice(nsig, size=min(args.plain_signals // 3, nsig), replace=False))
+    s = wc.default_stream()
+    for loss_name, loss in (("sure", wc.LOSS_SURE), ("cv", wc.LOSS_CV)):
+        for prec in (2, 1):
+            opts = wc.fit_opts(loss_type=loss, iterations=60, precision=prec, smooth=True)
+            res = (wc.FitResult * nsig)()
+            buf = wc.DeviceBuffer(X.nbytes)
+            buf.upload(X, s)     # warm-up run (workspace growth), then the timed one
+            wc.check(L.wc_fit_thresholds_device(buf.ptr, n, nsig, J, wc.LA8, 1, C.byref(opts),
+                                                res, s))
+            buf.upload(X, s)
+            e0, e1 = wc.Event(), wc.Event()
+            e0.record(s)
+            wc.check(L.wc_fit_thresholds_device(buf.ptr, n, nsig, J, wc.LA8, 1, C.byref(opts),
+                                                res, s))
+            e1.record(s)
+            wc.check(L.wc_stream_synchronize(s))
+            dev_ms = e0.elapsed_ms(e1)
+            y = buf.download(np.float64, X.size, s).reshape(nsig, n)
+            buf.free()
+            t0 = time.perf_counter()
+            wc.fit_thresholds(X, J, wc.LA8, 1, loss_type=loss, iterations=60, precision=prec)
+            e2e_s = time.perf_counter() - t0
+            mse = np.mean((y - clean) ** 2, axis=1)
+            out[f"{loss_name}/{PREC[prec]}"] = {
+                "signals_s": nsig / (dev_ms / 1e3), "device_ms": dev_ms,
+                "e2e_signals_s": nsig / e2e_s, "mse_vs_clean": float(mse.mean()),
+                "mse_vs_clean_sample": float(mse[sub].mean()),
+                "loss_decrease": float(np.mean([1 - r.loss / r.loss0 if r.loss0 else 0
+                                                for r in res]))}
+    # plain per-signal golden-section CV smoothing (wc_smooth, host buffers)
+    for prec in (2, 1):
+        t0 = time.perf_counter()
+        ys = [wc.smooth(X[i], J, wc.MODWT, wc.LA8, wc.CV, 0.0, wc.SOFT, 0, J - 1, 1e-8, prec)[0]
+              for i in sub]
+        dt = time.perf_counter() - t0
+        out[f"plain_cv/{PREC[prec]}"] = {
+            "signals_s": len(sub) / dt,
+            "mse_vs_clean_sample": float(np.mean([np.mean((y - clean[i]) ** 2)
+                                                  for y, i in zip(ys, sub)])),
+            "sample": f"{len(sub)} random signals of the batch, one wc_smooth call each"}
+    for k in ("sure", "cv"):
+        for p in ("fp32", "fast"):
+            r = out[f"{k}/{p}"]
+            r["speedup_e2e_vs_plain"] = r["e2e_signals_s"] / out[f"plain_cv/{p}"]["signals_s"]
+    return out
+
+
 def reference(args):
     rank, world = dist_env()
     if rank != 0:
@@ -544,6 +611,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-signals", type=int, default=4096)
     ap.add_argument("--plain-signals", type=int, default=96)
+    ap.add_argument("--no-fit", action="store_true")
+    ap.add_argument("--fit-signals", type=int, default=256)
     ap.add_argument("--tiling", default=None,
                     help="tile:g0:threads:pipelined for --profile-case")
     ap.add_argument("--sweep-steps", type=int, default=2)

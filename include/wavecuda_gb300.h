@@ -296,6 +296,45 @@ WC_API int wc_loss_grad(const double* x, int64_t len, int nlevels, int filter, i
                         double sigma, double eps, double* loss, double* grad, double* sigma_used,
                         void* stream);
 
+/* Per-level soft-threshold tuning by gradient descent for a batch of nsig
+ * equal-length signals, all in one persistent launch (one CTA per signal
+ * at a time).  No counterpart in the reference: it fits one threshold per
+ * level, lambda_l = sigma u_l, to the SURE or the two-fold CV loss defined
+ * for wc_loss_grad, by `iterations` Adam steps on u through the adjoint
+ * kernels, keeps the best thresholds seen and (smooth != 0) overwrites each
+ * signal with its soft-thresholded reconstruction.  CV thresholds fitted on
+ * the half-length signals are rescaled by 1/sqrt(1 - log 2 / log len) for the
+ * full signal (thresh.cpp:326) and levels above nlevels-2 take the level
+ * nlevels-2 value.  Bulk arithmetic in `precision` (WC_F32, or WC_F64_FAST:
+ * FP64 data with double-float arithmetic); loss and gradient totals in FP64. */
+#define WC_FIT_MAX_LEVELS 24
+typedef struct {
+  int loss_type;          /* WC_LOSS_SURE or WC_LOSS_CV */
+  int minlevel, maxlevel; /* thresholded levels (0-based); maxlevel < 0: nlevels-1 */
+  int iterations;         /* Adam steps (the loss is evaluated iterations+1 times) */
+  double step;            /* Adam step in units of sigma, e.g. 0.1 */
+  double eps;             /* SURE: logistic width of the kept indicator in units of
+                             sigma (0: the indicator itself) */
+  double sigma;           /* noise level; <= 0: MAD of the finest details, per signal */
+  const double* lambda0;  /* nlevels starting thresholds, or NULL: sigma sqrt(2 log len) */
+  int precision;          /* WC_F32 or WC_F64_FAST */
+  int smooth;             /* 1: overwrite x with the smoothed signals */
+} wc_fit_opts;
+typedef struct {
+  double lambda[WC_FIT_MAX_LEVELS]; /* thresholds for the full signal (0 outside the range) */
+  double grad0[WC_FIT_MAX_LEVELS];  /* loss gradient at the starting thresholds */
+  double loss0, loss, sigma;        /* loss at the start, best loss, sigma used */
+  int iterations, status;           /* status 1: not tunable (e.g. sigma 0) */
+} wc_fit_result;
+/* x: device, nsig * len FP64 values (signal k at x + k*len); results: host,
+ * nsig records.  Synchronous. */
+WC_API int wc_fit_thresholds_device(double* x, int64_t len, int nsig, int nlevels, int filter,
+                                    int ttype, const wc_fit_opts* opts, wc_fit_result* results,
+                                    void* stream);
+/* Same with x in host memory (copied in and, when smoothing, back out). */
+WC_API int wc_fit_thresholds(double* x, int64_t len, int nsig, int nlevels, int filter, int ttype,
+                             const wc_fit_opts* opts, wc_fit_result* results);
+
 /* ---- runtime helpers (device memory, pinned host memory, timing) */
 WC_API int wc_device_count(int* count);
 WC_API int wc_malloc_device(void** ptr, size_t bytes);

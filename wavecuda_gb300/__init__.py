@@ -65,6 +65,22 @@ class SignalResult(C.Structure):
                 ("kept", C.c_int64), ("zeroed", C.c_int64)]
 
 
+FIT_MAX_LEVELS = 24
+
+
+class FitOpts(C.Structure):
+    _fields_ = [("loss_type", C.c_int), ("minlevel", C.c_int), ("maxlevel", C.c_int),
+                ("iterations", C.c_int), ("step", C.c_double), ("eps", C.c_double),
+                ("sigma", C.c_double), ("lambda0", C.POINTER(C.c_double)),
+                ("precision", C.c_int), ("smooth", C.c_int)]
+
+
+class FitResult(C.Structure):
+    _fields_ = [("lambda_", C.c_double * FIT_MAX_LEVELS), ("grad0", C.c_double * FIT_MAX_LEVELS),
+                ("loss0", C.c_double), ("loss", C.c_double), ("sigma", C.c_double),
+                ("iterations", C.c_int), ("status", C.c_int)]
+
+
 _lib: Optional[C.CDLL] = None
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -106,6 +122,10 @@ def lib() -> C.CDLL:
                                                    C.c_int, _dp, C.c_int, C.c_int, _vp]
     L.wc_loss_grad.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int,
                                C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _vp]
+    L.wc_fit_thresholds_device.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(FitOpts), C.POINTER(FitResult), _vp]
+    L.wc_fit_thresholds.argtypes = [_dp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.POINTER(FitOpts), C.POINTER(FitResult)]
     L.wc_batch_plan_create.argtypes = [C.POINTER(Signal), C.c_int, C.c_int, C.POINTER(_vp)]
     L.wc_batch_plan_destroy.argtypes = [_vp]
     L.wc_batch_plan_info.argtypes = [_vp, _ip, C.POINTER(C.c_size_t)]
@@ -472,6 +492,44 @@ def loss_grad(x, nlevels, filter, ttype, loss_type, lam, min_level=0, max_level=
     finally:
         buf.free()
     return loss.value, grad, sig.value
+
+
+def fit_opts(loss_type=LOSS_SURE, min_level=0, max_level=-1, iterations=60, step=0.1,
+             eps=0.1, sigma=0.0, lambda0=None, precision=F32, smooth=True):
+    """wc_fit_opts for fit_thresholds (lambda0 is kept alive on the record)."""
+    o = FitOpts(loss_type, min_level, max_level, iterations, step, eps, sigma, None, precision,
+                1 if smooth else 0)
+    if lambda0 is not None:
+        lam = np.ascontiguousarray(lambda0, dtype=np.float64)
+        o._lam = lam
+        o.lambda0 = lam.ctypes.data_as(_dp)
+    return o
+
+
+def fit_thresholds(x2d, nlevels, filter, ttype, device=False, **kw):
+    """Per-level soft thresholds fitted by gradient descent for a batch of
+    equal-length signals (rows of x2d), one persistent launch
+    (wc_fit_thresholds).  Returns (smoothed rows, list of FitResult)."""
+    x = np.array(x2d, dtype=np.float64, copy=True, order="C")
+    if x.ndim == 1:
+        x = x[None, :]
+    nsig, n = x.shape
+    opts = fit_opts(**kw)
+    res = (FitResult * nsig)()
+    if device:
+        buf = DeviceBuffer(x.nbytes)
+        buf.upload(x)
+        try:
+            check(lib().wc_fit_thresholds_device(buf.ptr, n, nsig, nlevels, filter, ttype,
+                                                 C.byref(opts), res, None))
+            y = buf.download(np.float64, x.size).reshape(nsig, n)
+        finally:
+            buf.free()
+    else:
+        check(lib().wc_fit_thresholds(x.ctypes.data_as(_dp), n, nsig, nlevels, filter, ttype,
+                                      C.byref(opts), res))
+        y = x
+    return y, list(res)
 
 
 def sequential_sum(v) -> float:

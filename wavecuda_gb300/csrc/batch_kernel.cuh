@@ -87,6 +87,21 @@ __device__ __forceinline__ typename P::V thr_v(typename P::V c, const Th<P>& th,
   return thr(c, th.t, th.hardness);
 }
 
+// One soft threshold per level (levels [minl, maxl]); the threshold tuner
+// keeps it in shared memory.
+constexpr int kLvMax = 24;  // = kFitLevels
+template <class P>
+struct ThL {
+  typename P::V t[kLvMax];
+  int minl, maxl;
+};
+
+template <class P>
+__device__ __forceinline__ typename P::V thr_v(typename P::V c, const ThL<P>& th, int l) {
+  if (l < th.minl || l > th.maxl) return c;
+  return thr(c, th.t[l], 1);
+}
+
 template <class P>
 __device__ __forceinline__ typename P::V to_v(double x) {
   if constexpr (std::is_same<typename P::V, dd>::value) return dd_from_double(x);
@@ -152,9 +167,9 @@ __device__ void bdwt_fwd(const S* y, typename P::T* out, int64_t N, int J, typen
 // they are read.  The coarse scaling slots q*2^J, q > 0, are read from
 // `coarse` (the reference's stale slots, thresh.cpp:15-35) or from w when
 // coarse == nullptr; slot 0 always from w.
-template <int F, class P, class D>
+template <int F, class P, class D, class TH>
 __device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_t N, int J,
-                         const Th<P>& th, typename P::V* tA, typename P::V* tB) {
+                         const TH& th, typename P::V* tA, typename P::V* tB) {
   using V = typename P::V;
   constexpr int L = filter_len(F);
   constexpr int H = L / 2;
@@ -258,9 +273,9 @@ __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, in
   }
 }
 
-template <int F, class P, class D>
+template <int F, class P, class D, class TH>
 __device__ void bmodwt_inv(const typename P::T* det, const typename P::T* sJ, D* out, int64_t N,
-                           int J, const Th<P>& th, typename P::V* tA, typename P::V* tB) {
+                           int J, const TH& th, typename P::V* tA, typename P::V* tB) {
   using V = typename P::V;
   constexpr int L = filter_len(F);
   for (int l = J - 1; l >= 0; l--) {
@@ -570,12 +585,12 @@ __device__ void fwd_any(int ttype, const S* s, typename P::T* w, typename P::T* 
   else bmodwt_fwd<F, P, S>(s, w, sJ, n, J, tA, tB);
 }
 
-template <int F, class P, class D>
+template <int F, class P, class D, class TH>
 __device__ void inv_any(int ttype, const typename P::T* w, const typename P::T* sJ,
-                        const D* coarse, D* out, int64_t n, int J, const Th<P>& th,
+                        const D* coarse, D* out, int64_t n, int J, const TH& th,
                         typename P::V* tA, typename P::V* tB) {
-  if (ttype == 0) bdwt_inv<F, P, D>(w, coarse, out, n, J, th, tA, tB);
-  else bmodwt_inv<F, P, D>(w, sJ, out, n, J, th, tA, tB);
+  if (ttype == 0) bdwt_inv<F, P, D, TH>(w, coarse, out, n, J, th, tA, tB);
+  else bmodwt_inv<F, P, D, TH>(w, sJ, out, n, J, th, tA, tB);
 }
 
 // univ_thresh (thresh.cpp:170-201) on the stored coefficients.
