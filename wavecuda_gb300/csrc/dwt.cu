@@ -45,20 +45,55 @@ __host__ __device__ constexpr int64_t fwd_halo(int L, int G, int l) {
   return (int64_t)(L - 2) * (((int64_t)1 << (G - l)) - 1);
 }
 
+// Two adjacent values p[0], p[1] with one vector shared-memory access (p is
+// aligned to two values: every pair below starts at an even index of a
+// 16-byte-aligned buffer).
+template <class V>
+__device__ __forceinline__ void ld2(const V* p, V& a, V& b) {
+  if constexpr (std::is_same<V, dd>::value) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    a = dd{t.x, t.y};
+    b = dd{t.z, t.w};
+  } else if constexpr (std::is_same<V, float>::value) {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    a = t.x;
+    b = t.y;
+  } else {
+    const double2 t = *reinterpret_cast<const double2*>(p);
+    a = t.x;
+    b = t.y;
+  }
+}
+
+template <class V>
+__device__ __forceinline__ void st2(V* p, V a, V b) {
+  if constexpr (std::is_same<V, dd>::value) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
+  } else if constexpr (std::is_same<V, float>::value) {
+    *reinterpret_cast<float2*>(p) = make_float2(a, b);
+  } else {
+    *reinterpret_cast<double2*>(p) = make_double2(a, b);
+  }
+}
+
 template <int F, class P>
 __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V& s,
                                          typename P::V& d) {
+  using V = typename P::V;
+  constexpr int L = filter_len(F);
+  V v[L];
+#pragma unroll
+  for (int j = 0; j < L; j += 2) ld2(src + j, v[j], v[j + 1]);
   if constexpr (F == 1) {
-    s = haar_sum<P>(src[0], src[1]);
-    d = haar_dif<P>(src[0], src[1]);
+    s = haar_sum<P>(v[0], v[1]);
+    d = haar_dif<P>(v[0], v[1]);
   } else {
-    constexpr int L = filter_len(F);
-    typename P::Acc as = P::acc_init(src[0], tap_h(F, 0));
-    typename P::Acc ad = P::acc_init(src[0], tap_g(F, 0));
+    typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
+    typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
 #pragma unroll
     for (int j = 1; j < L; j++) {
-      as = P::acc_add(as, src[j], tap_h(F, j));
-      ad = P::acc_add(ad, src[j], tap_g(F, j));
+      as = P::acc_add(as, v[j], tap_h(F, j));
+      ad = P::acc_add(ad, v[j], tap_g(F, j));
     }
     s = P::acc_fin(as);
     d = P::acc_fin(ad);
@@ -102,12 +137,12 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     const bool ok = mbar_wait(&bar, 0, status);
     if (__syncthreads_or(!ok)) return;
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+      for (int m = threadIdx.x; m < (int)(Tt + H0); m += blockDim.x)
         A[m] = P::ld(reinterpret_cast<const T*>(A)[m]);
       __syncthreads();
     }
   } else {
-    for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+    for (int m = threadIdx.x; m < (int)(Tt + H0); m += blockDim.x)
       A[m] = P::ld(in[wrap(t0 + m, N)]);
     __syncthreads();
   }
@@ -115,10 +150,10 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
   V* src = A;
   V* dst = B;
   for (int l = 1; l <= G; l++) {
-    const int64_t nD = Tt >> l;
-    const int64_t nS = nD + fwd_halo(L, G, l);
-    const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
-    for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+    const int nD = (int)(Tt >> l);
+    const int nS = nD + (int)fwd_halo(L, G, l);
+    const int dstep = 1 << l, doff = 1 << (l - 1);
+    for (int k = threadIdx.x; k < nS; k += blockDim.x) {
       V s, d;
       fwd_pair<F, P>(src + 2 * k, s, d);
       dst[k] = s;
@@ -127,8 +162,8 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     __syncthreads();
     V* t = src; src = dst; dst = t;
   }
-  const int64_t nC = Tt >> G;
-  for (int64_t k = threadIdx.x; k < nC; k += blockDim.x) {
+  const int nC = (int)(Tt >> G);
+  for (int k = threadIdx.x; k < nC; k += blockDim.x) {
     Z[k << G] = src[k];
     if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
   }
@@ -136,7 +171,7 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
   if (bulk && S == 1) {
     T* Zt = reinterpret_cast<T*>(Z);
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+      for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
         const V v = Z[m];
         Zt[m] = P::st(v);
       }
@@ -151,7 +186,7 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     return;
   }
   const int64_t cmask = ((int64_t)1 << G) - 1;
-  for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+  for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
     if (write_coarse_slots || (m & cmask) != 0) out[(t0 + m) * S] = P::st(Z[m]);
   }
 }
@@ -198,17 +233,18 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     const bool ok = mbar_wait(&bar, 0, status);
     if (__syncthreads_or(!ok)) return;
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+      for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
         Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
     }
   } else {
-    for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+    for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
       Z[m] = P::ld(det[wrap(t0 - H + m, N) * S]);
   }
   {
-    const int64_t NG = N >> G, q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
+    const int64_t NG = N >> G, q0 = t0 >> G;
+    const int cnt = (int)(Tt >> G) + geo.need[G];
     V* buf = (G & 1) ? SB : SA;  // level-G buffer; level 0 ends in SA
-    for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x)
       buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG) * cstride]);
   }
   __syncthreads();
@@ -217,10 +253,10 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     V* src = (l & 1) ? SB : SA;
     V* dst = (l & 1) ? SA : SB;
     const int P_l = (geo.need[l - 1] + 1) >> 1;
-    const int64_t nq = (Tt >> l) + P_l;
-    const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
-    for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
-      const int64_t qr = k - P_l;  // q - q0
+    const int nq = (int)(Tt >> l) + P_l;
+    const int dstep = 1 << l, doff = (1 << (l - 1)) + (int)H;
+    for (int k = threadIdx.x; k < nq; k += blockDim.x) {
+      const int qr = k - P_l;  // q - q0
       constexpr int HH = filter_len(F) / 2;
       V sv[HH], dv[HH];
 #pragma unroll
@@ -248,15 +284,14 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
         e = P::acc_fin(ae);
         o = P::acc_fin(ao);
       }
-      dst[2 * qr + geo.off[l - 1]] = e;
-      dst[2 * qr + 1 + geo.off[l - 1]] = o;
+      st2(dst + 2 * qr + geo.off[l - 1], e, o);
     }
     __syncthreads();
   }
   if (bulk && ostride == 1) {
     T* St = reinterpret_cast<T*>(SA);
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+      for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
         const V v = SA[m];
         St[m] = P::st(v);
       }
@@ -270,7 +305,7 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     }
     return;
   }
-  for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x)
+  for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x)
     outp[(t0 + m) * ostride] = P::st(SA[m + geo.off[0]]);
 }
 
@@ -333,17 +368,17 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     }
     V* A = b ? R1 : R0;
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt + H0; m += blockDim.x)
+      for (int m = threadIdx.x; m < (int)(Tt + H0); m += blockDim.x)
         A[m] = P::ld(reinterpret_cast<const T*>(A)[m]);
       __syncthreads();
     }
     V* src = A;
     V* dst = B;
     for (int l = 1; l <= G; l++) {
-      const int64_t nD = Tt >> l;
-      const int64_t nS = nD + fwd_halo(L, G, l);
-      const int64_t dstep = (int64_t)1 << l, doff = (int64_t)1 << (l - 1);
-      for (int64_t k = threadIdx.x; k < nS; k += blockDim.x) {
+      const int nD = (int)(Tt >> l);
+      const int nS = nD + (int)fwd_halo(L, G, l);
+      const int dstep = 1 << l, doff = 1 << (l - 1);
+      for (int k = threadIdx.x; k < nS; k += blockDim.x) {
         V s, d;
         fwd_pair<F, P>(src + 2 * k, s, d);
         dst[k] = s;
@@ -352,15 +387,15 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
       __syncthreads();
       V* t = src; src = dst; dst = t;
     }
-    const int64_t nC = Tt >> G;
-    for (int64_t k = threadIdx.x; k < nC; k += blockDim.x) {
+    const int nC = (int)(Tt >> G);
+    for (int k = threadIdx.x; k < nC; k += blockDim.x) {
       Z[k << G] = src[k];
       if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
     }
     __syncthreads();
     T* Zt = reinterpret_cast<T*>(Z);
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+      for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
         const V v = Z[m];
         Zt[m] = P::st(v);
       }
@@ -437,13 +472,14 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
     }
     V* Z = b ? Z1 : Z0;
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt + H; m += blockDim.x)
+      for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
         Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
     }
     {
-      const int64_t q0 = t0 >> G, cnt = (Tt >> G) + geo.need[G];
+      const int64_t q0 = t0 >> G;
+      const int cnt = (int)(Tt >> G) + geo.need[G];
       V* buf = (G & 1) ? SB : SA;
-      for (int64_t k = threadIdx.x; k < cnt; k += blockDim.x)
+      for (int k = threadIdx.x; k < cnt; k += blockDim.x)
         buf[k] = P::ld(coarse[wrap(q0 - geo.need[G] + k, NG) * cstride]);
     }
     __syncthreads();
@@ -451,10 +487,10 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
       V* src = (l & 1) ? SB : SA;
       V* dst = (l & 1) ? SA : SB;
       const int P_l = (geo.need[l - 1] + 1) >> 1;
-      const int64_t nq = (Tt >> l) + P_l;
-      const int64_t dstep = (int64_t)1 << l, doff = ((int64_t)1 << (l - 1)) + H;
-      for (int64_t k = threadIdx.x; k < nq; k += blockDim.x) {
-        const int64_t qr = k - P_l;
+      const int nq = (int)(Tt >> l) + P_l;
+      const int dstep = 1 << l, doff = (1 << (l - 1)) + (int)H;
+      for (int k = threadIdx.x; k < nq; k += blockDim.x) {
+        const int qr = k - P_l;
         V sv[HH], dv[HH];
 #pragma unroll
         for (int j = 0; j < HH; j++) {
@@ -480,14 +516,13 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
           e = P::acc_fin(ae);
           o = P::acc_fin(ao);
         }
-        dst[2 * qr + geo.off[l - 1]] = e;
-        dst[2 * qr + 1 + geo.off[l - 1]] = o;
+        st2(dst + 2 * qr + geo.off[l - 1], e, o);
       }
       __syncthreads();
     }
     T* St = reinterpret_cast<T*>(SA);
     if constexpr (!std::is_same<T, V>::value) {
-      for (int64_t m = threadIdx.x; m < Tt; m += blockDim.x) {
+      for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
         const V v = SA[m];
         St[m] = P::st(v);
       }
@@ -574,9 +609,18 @@ bool g_cfg_set[5][3] = {};
 
 int gmax_of(int F) { return F == 1 ? 12 : F == 2 ? 8 : F == 3 ? 7 : 6; }
 
+// Defaults: the fastest candidates of wc_tune_dwt on a GB300 at n = 2^24
+// (forward + inverse), per filter and precision (exact, fast, FP32).
 TileCfg default_cfg(int F, int prec) {
-  const int tile = (prec == WC_F32) ? 8192 : 4096;
-  return TileCfg{tile, gmax_of(F), 512, 1};
+  static const TileCfg table[5][3] = {
+      {{4096, 8, 512, 1}, {4096, 8, 512, 1}, {8192, 8, 512, 1}},
+      {{2048, 11, 256, 0}, {2048, 11, 512, 0}, {4096, 12, 256, 1}},  // Haar
+      {{4096, 7, 512, 0}, {2048, 7, 256, 0}, {4096, 8, 256, 1}},     // D4
+      {{4096, 7, 512, 0}, {2048, 6, 512, 0}, {4096, 6, 256, 1}},     // C6
+      {{4096, 5, 256, 0}, {2048, 5, 512, 0}, {4096, 5, 512, 0}},     // LA8
+  };
+  if (F < 1 || F > 4 || prec < 0 || prec > 2) return TileCfg{4096, gmax_of(F), 512, 1};
+  return table[F][prec];
 }
 
 TileCfg get_cfg(int F, int prec) {
