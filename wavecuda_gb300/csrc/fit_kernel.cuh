@@ -91,6 +91,7 @@ __device__ void badj_modwt(const typename P::V* g, const typename P::T* det, int
                            typename P::V* tB, FitShared<P>& sh) {
   using V = typename P::V;
   constexpr int L = filter_len(F);
+  const int64_t B = blockDim.x;
   for (int l = 0; l <= maxl; l++) {
     const V* src = (l == 0) ? g : ((l & 1) ? tA : tB);
     V* dst = (l & 1) ? tB : tA;
@@ -100,42 +101,54 @@ __device__ void badj_modwt(const typename P::V* g, const typename P::T* det, int
     const bool need_s = l < maxl;
     const float lam = (float)sh.lam[l];
     float pg = 0.f, pk = 0.f, pdk = 0.f;
-    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
-      V s, d;
-      if constexpr (F == 1) {
-        const V a = src[i], b = src[(i + skip) & (N - 1)];
-        d = haar_dif<P>(a, b);
-        s = haar_sum<P>(a, b);
-      } else {
-        V v = src[i];
-        typename P::Acc ad = P::acc_init(v, tap_g(F, 0)), as = P::acc_init(v, tap_h(F, 0));
+    sweep_outputs<mod_unroll<V>()>(N, [&](auto uc, int64_t i0) {
+      constexpr int UU = decltype(uc)::value;
+      V v[UU][L];
+      float cv[UU];
 #pragma unroll
-        for (int k = 1; k < L; k++) {
-          v = src[(i + (int64_t)k * skip) & (N - 1)];
-          ad = P::acc_add(ad, v, tap_g(F, k));
-          as = P::acc_add(as, v, tap_h(F, k));
-        }
-        d = P::acc_fin(ad);
-        s = P::acc_fin(as);
+      for (int u = 0; u < UU; u++) {
+        const int64_t i = i0 + u * B;
+#pragma unroll
+        for (int k = 0; k < L; k++) v[u][k] = src[(i + (int64_t)k * skip) & (N - 1)];
+        cv[u] = acc ? tf(cl[i]) : 0.f;
       }
-      if (need_s) dst[i] = s;
-      if (acc) {
-        const float c = tf(cl[i]), ac = fabsf(c);
-        if (!(ac < lam)) {
-          const float dv = vhi(d);
-          pg += (c < 0.f) ? dv : -dv;
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
+        const int64_t i = i0 + u * B;
+        V s, d;
+        if constexpr (F == 1) {
+          d = haar_dif<P>(v[u][0], v[u][1]);
+          s = haar_sum<P>(v[u][0], v[u][1]);
+        } else {
+          typename P::Acc ad = P::acc_init(v[u][0], tap_g(F, 0));
+          typename P::Acc as = P::acc_init(v[u][0], tap_h(F, 0));
+#pragma unroll
+          for (int k = 1; k < L; k++) {
+            ad = P::acc_add(ad, v[u][k], tap_g(F, k));
+            as = P::acc_add(as, v[u][k], tap_h(F, k));
+          }
+          d = P::acc_fin(ad);
+          s = P::acc_fin(as);
         }
-        if (div) {
-          if (inv_eps > 0.f) {
-            const float phi = 1.f / (1.f + __expf(-(ac - lam) * inv_eps));
-            pk += phi;
-            pdk += phi * (1.f - phi);
-          } else if (!(ac < lam)) {
-            pk += 1.f;
+        if (need_s) dst[i] = s;
+        if (acc) {
+          const float c = cv[u], ac = fabsf(c);
+          if (!(ac < lam)) {
+            const float dv = vhi(d);
+            pg += (c < 0.f) ? dv : -dv;
+          }
+          if (div) {
+            if (inv_eps > 0.f) {
+              const float phi = 1.f / (1.f + __expf(-(ac - lam) * inv_eps));
+              pk += phi;
+              pdk += phi * (1.f - phi);
+            } else if (!(ac < lam)) {
+              pk += 1.f;
+            }
           }
         }
       }
-    }
+    });
     if (acc) {
       block_add(&sh.g[l], pg);
       if (div) {
