@@ -382,6 +382,8 @@ def ours(args):
         out["batched"] = batch_bench(wc, args)
     if not args.no_fit:
         out["tuned"] = fit_bench(wc, args)
+    if not args.no_smooth:
+        out["smooth"] = smooth_bench(wc, args)
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -469,6 +471,41 @@ def batch_bench(wc, args):
         r["mse_vs_clean"] = mse
         r["cv_iterations_mean"] = float(np.mean([x.iterations for x in res if x.iterations]))
         out[PREC[prec]] = r
+    return out
+
+
+def smooth_bench(wc, args):
+    """GPUSmooth plain (exact FP64) against its precision forms: MODWT Haar
+    and LA8, 10 levels, soft, two-fold CV (golden section, tol 1e-8), levels
+    1..10 (0..9 in C), n = 2^20 signals shaped like doppler/blocks/bumps/
+    heavisine at SNR 3 and 7; one wc_smooth call per signal."""
+    from wavecuda_gb300 import signals as sg
+    n, J = 1 << args.smooth_log2n, 10
+    sigs = []
+    for i, shape in enumerate(sg.SHAPES):
+        f = sg.SHAPES[shape](n, i)
+        for snr in (3.0, 7.0):
+            sigs.append((f, sg.noisy(f, snr, seed=900 + 2 * i + int(snr))))
+    out = {"workload": f"{len(sigs)} signals, n = 2^{args.smooth_log2n}, MODWT, J = 10, soft, "
+                       "CV tol 1e-8, levels 0..9"}
+    for fname, filt in (("Haar", wc.HAAR), ("LA8", wc.LA8)):
+        ref_t = None
+        for prec in (0, 1, 2):
+            ts, mses, ths, its = [], [], [], []
+            for f, x in sigs:
+                t0 = time.perf_counter()
+                y, info = wc.smooth(x, J, wc.MODWT, filt, wc.CV, 0.0, wc.SOFT, 0, J - 1, 1e-8, prec)
+                ts.append(time.perf_counter() - t0)
+                mses.append(float(np.mean((y - f) ** 2)))
+                ths.append(info.thresh)
+                its.append(info.iterations)
+            if prec == 0:
+                ref_t = ths
+            out[f"{fname}/{PREC[prec]}"] = {
+                "signals_s": len(sigs) / sum(ts), "ms_per_signal": 1e3 * sum(ts) / len(sigs),
+                "mse_vs_clean": float(np.mean(mses)), "cv_iterations": float(np.mean(its)),
+                "thresh_rel_diff_vs_exact": float(max(abs(a - b) / abs(b)
+                                                      for a, b in zip(ths, ref_t)))}
     return out
 
 
@@ -612,6 +649,8 @@ def main():
     ap.add_argument("--batch-signals", type=int, default=4096)
     ap.add_argument("--plain-signals", type=int, default=96)
     ap.add_argument("--no-fit", action="store_true")
+    ap.add_argument("--no-smooth", action="store_true")
+    ap.add_argument("--smooth-log2n", type=int, default=20)
     ap.add_argument("--fit-signals", type=int, default=256)
     ap.add_argument("--tiling", default=None,
                     help="tile:g0:threads:pipelined for --profile-case")

@@ -142,3 +142,52 @@ def test_errors_are_status_codes(gpu):
         gpu.transform(y, 11, gpu.DWT, gpu.HAAR)          # too many levels
     with pytest.raises(gpu.WaveCudaError):
         gpu.transform(np.zeros(1000), 2, gpu.DWT, gpu.HAAR)  # not a power of two
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("filt", FILTERS)
+def test_host_streamed_dwt_matches_device_path(gpu, oracle, filt, prec):
+    """Long DWTs on host arrays stream over the host link in chunks, with the
+    first pass writing into host memory; the result must be the device
+    path's (bit-identical in exact FP64), forward and inverse, for pageable
+    (numpy) and pinned host arrays."""
+    L = gpu.lib()
+    for n in (1 << 22, 1 << 23):
+        x = signals.roofline_input(n, seed=n + filt)
+        for J in sorted({1, 7, oracle.levels(n, 0, filt)}):
+            a, b = gpu.DeviceBuffer(8 * n), gpu.DeviceBuffer(8 * n)
+            a.upload(x)
+            gpu.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, J, filt, prec, None))
+            gpu.check(L.wc_stream_synchronize(None))
+            w_dev = b.download(np.float64, n)
+            gpu.check(L.wc_dwt_device(b.ptr, a.ptr, n, 0, J, filt, prec, None))
+            gpu.check(L.wc_stream_synchronize(None))
+            r_dev = a.download(np.float64, n)
+            a.free(); b.free()
+            w = gpu.transform(x, J, gpu.DWT, filt, gpu.FWD, prec)
+            r = gpu.transform(w, J, gpu.DWT, filt, gpu.BWD, prec)
+            if prec == 0:
+                assert np.array_equal(w, w_dev), (n, J)
+                assert np.array_equal(r, r_dev), (n, J)
+            else:
+                assert rel_err(w, w_dev) <= 1e-13 and rel_err(r, r_dev) <= 1e-13, (n, J)
+        if prec == 0 and n == 1 << 22:
+            assert np.array_equal(w, oracle.dwt(x, J, filt))
+    # pinned host memory through the reference-facing symbol
+    n, J = 1 << 22, 9
+    x = signals.roofline_input(n, seed=5)
+    h = gpu.HostBuffer(n)
+    h.array[:] = x
+    gpu.set_default_precision(prec)
+    try:
+        import ctypes as C
+        args = [C.c_int(v) for v in (n, 1, J, 0, filt, P.FILTER_LEN[filt])]
+        dummy = np.zeros(1)
+        xp = C.cast(h.ptr, C.POINTER(C.c_double))
+        L.RgpuTransform(xp, dummy.ctypes.data_as(C.POINTER(C.c_double)),
+                        *[C.byref(v) for v in args])
+        ref = gpu.transform(x, J, gpu.DWT, filt, gpu.FWD, prec)
+        assert np.array_equal(h.array, ref)
+    finally:
+        gpu.set_default_precision(0)
+        h.free()

@@ -232,7 +232,32 @@ int convert(const A* in, B* out, int64_t n, cudaStream_t s) {
   return after_launch("convert_k");
 }
 
-// Host-buffer transform: stage in HBM, run, copy back.
+// Signals at least this long are streamed over the host link in chunks
+// (dwt_host_inplace) when the GPU can address the host array.
+constexpr int64_t kHostStreamMin = (int64_t)1 << 22;
+
+// True when kernels may dereference the host pointer p: memory registered
+// with (or allocated by) CUDA and mapped at the same address, or pageable
+// memory on a system whose GPU reads the host page tables.
+bool device_addressable(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+  if (a.type != cudaMemoryTypeUnregistered) return false;
+  int dev = 0, pageable = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return pageable == 1;
+}
+
+// Host-buffer transform: stage in HBM, run, copy back (long DWTs stream
+// instead, see dwt_host_inplace).
 int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels, int ttype,
                    int filter, int filterlen, int prec) {
   WC_TRY(ensure_device());
@@ -261,6 +286,14 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
     if (!f) return workspace_error();
     fa = reinterpret_cast<float*>(f);
     fb = reinterpret_cast<float*>(f + abytes);
+  }
+  if (ttype == 0 && prec != WC_F32 && len >= kHostStreamMin && device_addressable(x)) {
+    const int r = dwt_host_inplace(x, len, sense, J, filter, prec, s);
+    if (r != WC_ERR_UNSUPPORTED) {
+      WC_TRY(r);
+      WC_CUDA(cudaStreamSynchronize(s));
+      return WC_OK;
+    }
   }
   if (ttype == 0) {
     WC_CUDA(cudaMemcpyAsync(A, x, bx, cudaMemcpyHostToDevice, s));

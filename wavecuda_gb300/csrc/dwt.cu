@@ -87,6 +87,12 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
   if constexpr (F == 1) {
     s = haar_sum<P>(v[0], v[1]);
     d = haar_dif<P>(v[0], v[1]);
+  } else if constexpr (std::is_same<P, PDD>::value) {
+    // s in lane 0, d in lane 1: the same operations as below, packed.
+    dd_acc2 A = acc2_init(v[0], make_tap2(tap_h(F, 0), tap_g(F, 0)));
+#pragma unroll
+    for (int j = 1; j < L; j++) A = acc2_add(A, v[j], make_tap2(tap_h(F, j), tap_g(F, j)));
+    acc2_fin(A, s, d);
   } else {
     typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
     typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
@@ -100,17 +106,55 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
   }
 }
 
+// Inverse step of one pair: even and odd outputs from s[-j] and d[-j]
+// (sv/dv in ascending j), taps in descending j as daub4.cpp:58-88.
+template <int F, class P>
+__device__ __forceinline__ void inv_pair(const typename P::V* sv, const typename P::V* dv,
+                                         typename P::V& e, typename P::V& o) {
+  constexpr int HH = filter_len(F) / 2;
+  if constexpr (F == 1) {
+    e = haar_sum<P>(sv[0], dv[0]);
+    o = haar_dif<P>(sv[0], dv[0]);
+  } else if constexpr (std::is_same<P, PDD>::value) {
+    // e in lane 0, o in lane 1: the same operations as below, packed.
+    dd_acc2 A = acc2_init(sv[HH - 1], make_tap2(tap_h(F, 2 * (HH - 1)), tap_h(F, 2 * (HH - 1) + 1)));
+    A = acc2_add(A, dv[HH - 1], make_tap2(tap_g(F, 2 * (HH - 1)), tap_g(F, 2 * (HH - 1) + 1)));
+#pragma unroll
+    for (int j = HH - 2; j >= 0; j--) {
+      A = acc2_add(A, sv[j], make_tap2(tap_h(F, 2 * j), tap_h(F, 2 * j + 1)));
+      A = acc2_add(A, dv[j], make_tap2(tap_g(F, 2 * j), tap_g(F, 2 * j + 1)));
+    }
+    acc2_fin(A, e, o);
+  } else {
+    typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+    typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+    ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+    ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+    for (int j = HH - 2; j >= 0; j--) {
+      ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+      ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+      ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+      ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+    }
+    e = P::acc_fin(ae);
+    o = P::acc_fin(ao);
+  }
+}
+
 // Forward pass.  y[m] = in[m] (m < N, compact).  Writes the tile's
 // interleaved result to out[(t0+m)*S] and its level-G scaling values to
-// coarse[t0/2^G + k] (when coarse != nullptr).  With `bulk` set, the tile and
-// its halo arrive by bulk copies (one or two: the halo of the last tile wraps
-// to the start) and, for S == 1, the result leaves by one bulk store.
+// coarse[t0/2^G + k] (when coarse != nullptr).  With bit 0 of `bulk` set,
+// the tile and its halo arrive by bulk copies (one or two: the halo of the
+// last tile wraps to the start); with bit 1 set and S == 1, the result leaves
+// by one bulk store (plain stores otherwise, e.g. into host memory).  Block b
+// handles tile tile0 + b.
 template <int F, class P>
 __global__ void __launch_bounds__(kThreads)
 dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
              typename P::T* __restrict__ out, int64_t S,
              typename P::T* __restrict__ coarse, int write_coarse_slots, int bulk,
-             unsigned int* status) {
+             unsigned int* status, int64_t tile0) {
   using V = typename P::V;
   using T = typename P::T;
   constexpr int L = filter_len(F);
@@ -120,9 +164,9 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
   V* A = reinterpret_cast<V*>(smem_raw);
   V* B = A + pad16<V>(Tt + H0);
   V* Z = B + pad16<V>(Tt / 2 + fwd_halo(L, G, 1));
-  const int64_t t0 = (int64_t)blockIdx.x * Tt;
+  const int64_t t0 = (tile0 + (int64_t)blockIdx.x) * Tt;
 
-  if (bulk) {
+  if (bulk & 1) {
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -168,7 +212,7 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     if (coarse) coarse[(t0 >> G) + k] = P::st(src[k]);
   }
   __syncthreads();
-  if (bulk && S == 1) {
+  if ((bulk & 2) && S == 1) {
     T* Zt = reinterpret_cast<T*>(Z);
     if constexpr (!std::is_same<T, V>::value) {
       for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
@@ -194,7 +238,9 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
 // Inverse pass: reconstructs y[t0 .. t0+Tt) of the compact level sequence
 // (length N) from the level-G scaling values (coarse, length N/2^G, stride
 // cstride) and the details of levels 1..G stored at det[m*S] (m = 2^(l-1) mod
-// 2^l).  Writes outp[(t0+m)*ostride].
+// 2^l).  Writes outp[(t0+m)*ostride].  `bulk` bit 0: bulk-copy staging of
+// det (S == 1); bit 1: bulk store of the tile (ostride == 1).  Block b
+// handles tile tile0 + b.
 struct InvGeom {
   int need[24];  // left halo at level l (coefficients)
   int off[24];   // buffer offset of level l
@@ -205,7 +251,7 @@ __global__ void __launch_bounds__(kThreads)
 dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
              const typename P::T* __restrict__ det, int64_t S, int64_t N, int G,
              int64_t Tt, typename P::T* __restrict__ outp, int64_t ostride,
-             InvGeom geo, int bulk, unsigned int* status) {
+             InvGeom geo, int bulk, unsigned int* status, int64_t tile0) {
   using V = typename P::V;
   using T = typename P::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -214,9 +260,9 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
   V* Z = reinterpret_cast<V*>(smem_raw);
   V* SA = Z + pad16<V>(Tt + H);
   V* SB = SA + pad16<V>(Tt + 2 * geo.off[0] + 16);
-  const int64_t t0 = (int64_t)blockIdx.x * Tt;
+  const int64_t t0 = (tile0 + (int64_t)blockIdx.x) * Tt;
 
-  if (bulk) {
+  if (bulk & 1) {
     // S == 1: the staged range [t0-H, t0+Tt) is contiguous except that the
     // first tile's halo wraps to the end of the array.
     if (threadIdx.x == 0) mbar_init(&bar, 1);
@@ -265,30 +311,12 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
         dv[j] = Z[(qr - j) * dstep + doff];
       }
       V e, o;
-      // inv_pair addresses s[-j] / d[-j]; sv/dv are stored in ascending j.
-      if constexpr (F == 1) {
-        e = haar_sum<P>(sv[0], dv[0]);
-        o = haar_dif<P>(sv[0], dv[0]);
-      } else {
-        typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
-        typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
-        ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
-        ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
-#pragma unroll
-        for (int j = HH - 2; j >= 0; j--) {
-          ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
-          ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
-          ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
-          ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
-        }
-        e = P::acc_fin(ae);
-        o = P::acc_fin(ao);
-      }
+      inv_pair<F, P>(sv, dv, e, o);
       st2(dst + 2 * qr + geo.off[l - 1], e, o);
     }
     __syncthreads();
   }
-  if (bulk && ostride == 1) {
+  if ((bulk & 2) && ostride == 1) {
     T* St = reinterpret_cast<T*>(SA);
     if constexpr (!std::is_same<T, V>::value) {
       for (int m = threadIdx.x; m < (int)Tt; m += blockDim.x) {
@@ -498,24 +526,7 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
           dv[j] = Z[(qr - j) * dstep + doff];
         }
         V e, o;
-        if constexpr (F == 1) {
-          e = haar_sum<P>(sv[0], dv[0]);
-          o = haar_dif<P>(sv[0], dv[0]);
-        } else {
-          typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
-          typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
-          ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
-          ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
-#pragma unroll
-          for (int j = HH - 2; j >= 0; j--) {
-            ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
-            ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
-            ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
-            ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
-          }
-          e = P::acc_fin(ae);
-          o = P::acc_fin(ao);
-        }
+        inv_pair<F, P>(sv, dv, e, o);
         st2(dst + 2 * qr + geo.off[l - 1], e, o);
       }
       __syncthreads();
@@ -546,6 +557,7 @@ struct PassPlan {
 };
 
 constexpr size_t kSmemBudget = 100 * 1024;
+constexpr int kHostChunksMax = 16;  // chunks of a host-streamed DWT
 
 template <class P>
 size_t fwd_smem(int L, int G, int64_t Tt) {
@@ -804,7 +816,7 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
         LaunchTimer lt(p == 0 ? "dwt_fwd_pass0" : "dwt_fwd_pass", s);
         kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, pp.S,
                                                              coarse, (last || pp.S == 1) ? 1 : 0,
-                                                             bulk, status);
+                                                             bulk ? 3 : 0, status, 0);
       }
       WC_TRY(after_launch("dwt_fwd_pass"));
       src = coarse;
@@ -833,8 +845,8 @@ int run_dwt(const void* vin, void* vout, int64_t n, int sense, int J, cudaStream
       {
         LaunchTimer lt(p == 0 ? "dwt_inv_pass0" : "dwt_inv_pass", s);
         kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(coarse, cstride, in, pp.S, pp.N,
-                                                             pp.G, pp.Tt, dst, 1, geo, bulk,
-                                                             status);
+                                                             pp.G, pp.Tt, dst, 1, geo, bulk ? 3 : 0,
+                                                             status, 0);
       }
       WC_TRY(after_launch("dwt_inv_pass"));
       coarse = dst;
@@ -865,6 +877,179 @@ int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
     case WC_F32: return dispatch_dwt<PF32>(in, out, n, sense, J, F, s);
   }
   return fail(WC_ERR_ARG, "unknown precision %d", prec);
+}
+
+// ---------------------------------------------------------------------------
+// Host-resident signals (the R entry points' case).  Copying the whole signal
+// in, transforming, and copying it back serialises two host-link transfers;
+// here the signal streams in by chunks on a second stream while the first
+// (forward) or last (inverse) pass of earlier chunks runs, and that pass
+// stores its tiles straight into host memory, so the link carries both
+// directions at once.  The coarse passes read (inverse) or write (forward)
+// their strided slots of the host array directly.  Needs a host array the
+// GPU can address (pinned, or pageable memory on a system whose GPU uses the
+// host page tables, such as Grace); callers check that.
+namespace {
+
+struct HostStreamState {
+  cudaStream_t up = nullptr;
+  cudaEvent_t ev[kHostChunksMax] = {};
+};
+std::mutex g_hs_mu;
+HostStreamState g_hs[64];
+
+int host_stream_state(HostStreamState** out) {
+  int dev = 0;
+  WC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(WC_ERR_UNSUPPORTED, "device ordinal %d", dev);
+  std::lock_guard<std::mutex> lk(g_hs_mu);
+  HostStreamState& st = g_hs[dev];
+  if (!st.up) {
+    WC_CUDA(cudaStreamCreateWithFlags(&st.up, cudaStreamNonBlocking));
+    for (int k = 0; k < kHostChunksMax; k++)
+      WC_CUDA(cudaEventCreateWithFlags(&st.ev[k], cudaEventDisableTiming));
+  }
+  *out = &st;
+  return WC_OK;
+}
+
+template <int F, class P>
+int run_dwt_host(typename P::T* x, int64_t n, int sense, int J, cudaStream_t s) {
+  using T = typename P::T;
+  const int L = filter_len(F);
+  TileCfg cfg = get_cfg(F, prec_of<P>());
+  cfg.pipe = 0;  // tile-offset launches of the per-tile kernels
+  std::vector<PassPlan> plan = plan_passes_cfg<P>(n, J, F, cfg);
+  const int np = (int)plan.size();
+  const PassPlan& p0 = plan[0];
+  const int64_t ntiles = p0.N / p0.Tt;
+  if (ntiles < 2) return WC_ERR_UNSUPPORTED;
+  const int K = (int)std::min<int64_t>(kHostChunksMax, ntiles);
+  const int64_t ct = ntiles / K, cs = ct * p0.Tt;  // tiles and values per chunk
+  const int64_t H0 = pad16<T>(fwd_halo(L, p0.G, 0));
+  const InvGeom geo0 = inv_geom(L, p0.G);
+  const int64_t HI = (int64_t)geo0.need[p0.G] << p0.G;
+  if (H0 > cs || HI > cs) return WC_ERR_UNSUPPORTED;
+  HostStreamState* hs = nullptr;
+  WC_TRY(host_stream_state(&hs));
+  unsigned int* status = device_status_word();
+  if (!status) return workspace_error();
+  T* A = static_cast<T*>(workspace(kSlotStageA, sizeof(T) * (size_t)n));
+  if (!A) return workspace_error();
+  T* scratch[2] = {nullptr, nullptr};
+  if (np > 1) {
+    const size_t cbytes = sizeof(T) * (size_t)(p0.N >> p0.G);
+    scratch[0] = static_cast<T*>(workspace(kSlotCoarse0, cbytes));
+    scratch[1] = static_cast<T*>(workspace(kSlotCoarse1, cbytes));
+    if (!scratch[0] || !scratch[1]) return workspace_error();
+  }
+  // The upload stream must not start before earlier work on s that may
+  // still read the staging buffer.
+  WC_CUDA(cudaEventRecord(hs->ev[0], s));
+  WC_CUDA(cudaStreamWaitEvent(hs->up, hs->ev[0], 0));
+  for (int k = 0; k < K; k++) {
+    WC_CUDA(cudaMemcpyAsync(A + k * cs, x + k * cs, sizeof(T) * (size_t)cs,
+                            cudaMemcpyHostToDevice, hs->up));
+    WC_CUDA(cudaEventRecord(hs->ev[k], hs->up));
+  }
+  const int ld_bulk = (aligned16_host(A) && (p0.Tt * (int64_t)sizeof(T)) % 16 == 0) ? 1 : 0;
+  if (sense == 1) {
+    T* coarse = (np > 1) ? scratch[0] : nullptr;
+    const size_t smem = fwd_smem<P>(L, p0.G, p0.Tt);
+    auto kern = dwt_fwd_pass<F, P>;
+    WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (int k = 0; k < K; k++) {
+      WC_CUDA(cudaStreamWaitEvent(s, hs->ev[k], 0));
+      WC_CUDA(cudaStreamWaitEvent(s, hs->ev[(k + 1) % K], 0));  // right halo
+      {
+        LaunchTimer lt("dwt_fwd_pass0", s);
+        kern<<<(unsigned)ct, kThreads, smem, s>>>(A, p0.N, p0.G, p0.Tt, x, 1, coarse, 1,
+                                                  (ld_bulk && H0 <= p0.N) ? 1 : 0, status,
+                                                  (int64_t)k * ct);
+      }
+      WC_TRY(after_launch("dwt_fwd_pass"));
+    }
+    const T* src = coarse;
+    for (int p = 1; p < np; p++) {
+      const PassPlan& pp = plan[p];
+      const bool last = (p == np - 1);
+      T* cn = last ? nullptr : scratch[p & 1];
+      const size_t sm = fwd_smem<P>(L, pp.G, pp.Tt);
+      const int64_t h0 = pad16<T>(fwd_halo(L, pp.G, 0));
+      const int b = (aligned16_host(src) && h0 <= pp.N && (pp.Tt * (int64_t)sizeof(T)) % 16 == 0)
+                        ? 1 : 0;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      {
+        LaunchTimer lt("dwt_fwd_pass", s);
+        kern<<<(unsigned)(pp.N / pp.Tt), kThreads, sm, s>>>(src, pp.N, pp.G, pp.Tt, x, pp.S, cn,
+                                                            last ? 1 : 0, b, status, 0);
+      }
+      WC_TRY(after_launch("dwt_fwd_pass"));
+      src = cn;
+    }
+    return WC_OK;
+  }
+  // Inverse: coarse passes straight from the host array, then the first
+  // pass chunk by chunk (chunk 0 last: its left halo wraps to the end).
+  auto ikern = dwt_inv_pass<F, P>;
+  const T* coarse = x;
+  int64_t cstride = plan[np - 1].S << plan[np - 1].G;
+  for (int p = np - 1; p >= 1; p--) {
+    const PassPlan& pp = plan[p];
+    T* dst = scratch[p & 1];
+    InvGeom geo = inv_geom(L, pp.G);
+    const size_t sm = inv_smem<P>(L, pp.G, pp.Tt);
+    WC_CUDA(cudaFuncSetAttribute(ikern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    {
+      LaunchTimer lt("dwt_inv_pass", s);
+      ikern<<<(unsigned)(pp.N / pp.Tt), kThreads, sm, s>>>(coarse, cstride, x, pp.S, pp.N, pp.G,
+                                                          pp.Tt, dst, 1, geo, 0, status, 0);
+    }
+    WC_TRY(after_launch("dwt_inv_pass"));
+    coarse = dst;
+    cstride = 1;
+  }
+  // A one-pass transform reads its coarse values from the staged copy: the
+  // chunks below overwrite the host array.
+  if (np == 1) coarse = A;
+  const size_t sm0 = inv_smem<P>(L, p0.G, p0.Tt);
+  WC_CUDA(cudaFuncSetAttribute(ikern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm0));
+  const int b0 = (ld_bulk && HI <= p0.N && (HI * (int64_t)sizeof(T)) % 16 == 0) ? 1 : 0;
+  for (int i = 1; i <= K; i++) {
+    const int k = i % K;
+    WC_CUDA(cudaStreamWaitEvent(s, hs->ev[k], 0));
+    WC_CUDA(cudaStreamWaitEvent(s, hs->ev[(k + K - 1) % K], 0));  // left halo
+    {
+      LaunchTimer lt("dwt_inv_pass0", s);
+      ikern<<<(unsigned)ct, kThreads, sm0, s>>>(coarse, cstride, A, 1, p0.N, p0.G, p0.Tt, x, 1,
+                                                geo0, b0, status, (int64_t)k * ct);
+    }
+    WC_TRY(after_launch("dwt_inv_pass"));
+  }
+  return WC_OK;
+}
+
+template <class P>
+int dispatch_dwt_host(void* x, int64_t n, int sense, int J, int F, cudaStream_t s) {
+  using T = typename P::T;
+  T* xt = static_cast<T*>(x);
+  switch (F) {
+    case 1: return run_dwt_host<1, P>(xt, n, sense, J, s);
+    case 2: return run_dwt_host<2, P>(xt, n, sense, J, s);
+    case 3: return run_dwt_host<3, P>(xt, n, sense, J, s);
+    case 4: return run_dwt_host<4, P>(xt, n, sense, J, s);
+  }
+  return fail(WC_ERR_ARG, "unknown filter %d", F);
+}
+
+}  // namespace
+
+int dwt_host_inplace(double* x, int64_t n, int sense, int J, int F, int prec, cudaStream_t s) {
+  switch (prec) {
+    case WC_F64_EXACT: return dispatch_dwt_host<PExact>(x, n, sense, J, F, s);
+    case WC_F64_FAST: return dispatch_dwt_host<PDD>(x, n, sense, J, F, s);
+  }
+  return WC_ERR_UNSUPPORTED;
 }
 
 }  // namespace wc
@@ -953,7 +1138,7 @@ int run_dwt_noalloc(const void* vin, void* vout, int64_t n, int sense, int J, cu
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(src, pp.N, pp.G, pp.Tt, out, pp.S,
                                                            coarse, (last || pp.S == 1) ? 1 : 0,
-                                                           bulk, status);
+                                                           bulk ? 3 : 0, status, 0);
       WC_TRY(after_launch("dwt_fwd_pass"));
       src = coarse;
     }
@@ -972,7 +1157,8 @@ int run_dwt_noalloc(const void* vin, void* vout, int64_t n, int sense, int J, cu
       auto kern = dwt_inv_pass<F, P>;
       WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       kern<<<(unsigned)(pp.N / pp.Tt), kThreads, smem, s>>>(coarse, cstride, in, pp.S, pp.N,
-                                                           pp.G, pp.Tt, dst, 1, geo, bulk, status);
+                                                           pp.G, pp.Tt, dst, 1, geo, bulk ? 3 : 0,
+                                                           status, 0);
       WC_TRY(after_launch("dwt_inv_pass"));
       coarse = dst;
       cstride = 1;

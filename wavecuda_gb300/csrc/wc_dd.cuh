@@ -155,4 +155,99 @@ struct PDD {
   static __device__ __forceinline__ V half(V a) { return {a.hi * 0.5f, a.lo * 0.5f}; }
 };
 
+// ---------------------------------------------------------------------------
+// Two Dot2 accumulators advanced together.  The sm_100-family packed FP32
+// instructions (add/sub/mul/fma .rn.f32x2) perform two IEEE FP32 operations
+// in one issue slot with the rounding of the scalar ones, so two dot
+// products of the same inputs with different taps -- a DWT level's scaling
+// and detail outputs, or the even and odd outputs of an inverse step -- cost
+// half the instructions of PDD::acc_* and give bit-identical pairs.
+// Lane 0 carries the first accumulator, lane 1 the second.  The error part
+// is kept negated (ne = -e), which lets every product error come from one
+// FMA against the negated tap and is exact under round-to-nearest symmetry.
+
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 x2_pack(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void x2_unpack(f32x2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f32x2 x2_add(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_sub(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_mul(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 x2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+struct dd_acc2 {
+  f32x2 s, ne;  // running sum of the high products; negated error sum
+};
+
+// Tap pair (c0 for lane 0, c1 for lane 1) split as for PDD: ch = fl32(c),
+// cl = fl32(c - ch).
+struct tap2 {
+  f32x2 ch, nch, ncl;
+};
+__device__ __forceinline__ tap2 make_tap2(double c0, double c1) {
+  const float h0 = (float)c0, h1 = (float)c1;
+  const float l0 = (float)(c0 - (double)h0), l1 = (float)(c1 - (double)h1);
+  return {x2_pack(h0, h1), x2_pack(-h0, -h1), x2_pack(-l0, -l1)};
+}
+
+// p = a.hi*ch (both lanes); negated product error -(a.hi*ch - p) - a.hi*cl
+// - a.lo*ch, accumulated as PDD::acc_init does (signs flipped).
+__device__ __forceinline__ dd_acc2 acc2_init(dd a, const tap2& c) {
+  const f32x2 ah = x2_pack(a.hi, a.hi), al = x2_pack(a.lo, a.lo);
+  const f32x2 p = x2_mul(ah, c.ch);
+  f32x2 ne = x2_fma(ah, c.nch, p);
+  ne = x2_fma(ah, c.ncl, ne);
+  ne = x2_fma(al, c.nch, ne);
+  return {p, ne};
+}
+
+__device__ __forceinline__ dd_acc2 acc2_add(dd_acc2 A, dd a, const tap2& c) {
+  const f32x2 ah = x2_pack(a.hi, a.hi), al = x2_pack(a.lo, a.lo);
+  const f32x2 p = x2_mul(ah, c.ch);
+  f32x2 npe = x2_fma(ah, c.nch, p);
+  npe = x2_fma(ah, c.ncl, npe);
+  npe = x2_fma(al, c.nch, npe);
+  // TwoSum(A.s, p) = (s, t)
+  const f32x2 s = x2_add(A.s, p);
+  const f32x2 bb = x2_sub(s, A.s);
+  const f32x2 t = x2_add(x2_sub(A.s, x2_sub(s, bb)), x2_sub(p, bb));
+  // e' = e + (pe + t)  <=>  ne' = ne + (npe - t)
+  return {s, x2_add(A.ne, x2_sub(npe, t))};
+}
+
+// Renormalised pairs: lane 0 -> r0, lane 1 -> r1 (PDD::acc_fin per lane).
+__device__ __forceinline__ void acc2_fin(dd_acc2 A, dd& r0, dd& r1) {
+  // TwoSum(s, e) with e = -ne: hi = s - ne; lo = (s - (hi - bb)) - (ne + bb)
+  const f32x2 hi = x2_sub(A.s, A.ne);
+  const f32x2 bb = x2_sub(hi, A.s);
+  const f32x2 lo = x2_sub(x2_sub(A.s, x2_sub(hi, bb)), x2_add(A.ne, bb));
+  float h0, h1, l0, l1;
+  x2_unpack(hi, h0, h1);
+  x2_unpack(lo, l0, l1);
+  r0 = {h0, l0};
+  r1 = {h1, l1};
+}
+
 }  // namespace wc

@@ -95,6 +95,13 @@ int check_levels(int64_t n, int nlevels, int filterlen);
 int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
         cudaStream_t s);
 
+// In-place DWT of a host array the GPU can address (FP64 data; exact or
+// double-float arithmetic), streamed over the host link in chunks.
+// Returns WC_ERR_UNSUPPORTED, with nothing enqueued, when the signal is too
+// short for chunking or the precision is FP32.  Enqueues on s; the caller
+// synchronises.
+int dwt_host_inplace(double* x, int64_t n, int sense, int J, int F, int prec, cudaStream_t s);
+
 // Time-ordered MODWT.  FWD: x -> xmod.  BWD: xmod -> x (xmod not modified).
 int modwt(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec,
           cudaStream_t s);
