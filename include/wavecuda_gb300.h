@@ -228,6 +228,19 @@ WC_API int wc_get_dwt_tiling(int filter, int precision, int* tile, int* g0, int*
                              int* pipelined);
 WC_API int wc_tune_dwt(int filter, int precision, int log2n, float* best_ms);
 
+/* Tiling of the MODWT level kernels per (filter, precision): values a tile
+ * aims at (a power of two in [256, 16384]) and the shared-memory budget per
+ * CTA (16..200 KB), for the forward and the inverse kernels.  wc_tune_modwt
+ * times every candidate on a 2^log2n-sample signal with nlevels levels and
+ * keeps the fastest per direction; the setting is per process.  No
+ * counterpart in the reference. */
+WC_API int wc_set_modwt_tiling(int filter, int precision, int fwd_target, int fwd_smem_kb,
+                               int inv_target, int inv_smem_kb);
+WC_API int wc_get_modwt_tiling(int filter, int precision, int* fwd_target, int* fwd_smem_kb,
+                               int* inv_target, int* inv_smem_kb);
+WC_API int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, float* fwd_ms,
+                         float* inv_ms);
+
 /* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
  * BWD reads only s_J and d_1..d_J. */
 WC_API int wc_modwt_device(void* x, void* xmod, int64_t len, int sense, int nlevels,

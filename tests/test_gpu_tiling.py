@@ -67,3 +67,26 @@ def test_autotune_keeps_a_valid_tiling(gpu, oracle):
     w = gpu.transform(x, 14, gpu.DWT, 2, gpu.FWD, 1)
     ref = oracle.dwt(x, 14, 2)
     assert np.max(np.abs(w - ref)) / np.max(np.abs(ref)) <= 1e-12
+
+
+@pytest.mark.parametrize("filt", [P.HAAR, P.D4, P.LA8])
+def test_modwt_tilings_match_oracle(gpu, oracle, filt):
+    """Every MODWT tile target and shared-memory budget gives the oracle's
+    result bit for bit in exact FP64 (forward and inverse)."""
+    n, J = 1 << 14, 9
+    x = np.random.default_rng(filt).standard_normal(n)
+    ref = oracle.modwt_fwd(x, J, filt)
+    keep = gpu.get_modwt_tiling(filt, 0)
+    try:
+        for target, kb in ((256, 16), (1024, 48), (4096, 96), (16384, 200)):
+            gpu.set_modwt_tiling(filt, 0, target, kb, target, kb)
+            xm = gpu.transform(x, J, gpu.MODWT, filt, gpu.FWD, gpu.F64_EXACT)
+            assert np.array_equal(xm, ref), (target, kb)
+            r = gpu.transform(xm, J, gpu.MODWT, filt, gpu.BWD, gpu.F64_EXACT, xmod=xm)
+            assert np.array_equal(r, oracle.modwt_inv(ref, n, J, filt)), (target, kb)
+        with pytest.raises(gpu.WaveCudaError):
+            gpu.set_modwt_tiling(filt, 0, 1000, 48, 1024, 48)
+        (t, f, i) = gpu.tune_modwt(filt, 1, 16, 8)
+        assert t[0] >= 256 and f > 0 and i > 0
+    finally:
+        gpu.set_modwt_tiling(filt, 0, *keep)

@@ -138,6 +138,10 @@ def lib() -> C.CDLL:
     L.wc_set_dwt_tiling.argtypes = [C.c_int] * 6
     L.wc_get_dwt_tiling.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
     L.wc_tune_dwt.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    L.wc_set_modwt_tiling.argtypes = [C.c_int] * 6
+    L.wc_get_modwt_tiling.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.wc_tune_modwt.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float),
+                                C.POINTER(C.c_float)]
     L.wc_device_count.argtypes = [_ip]
     L.wc_malloc_device.argtypes = [C.POINTER(_vp), C.c_size_t]
     L.wc_free_device.argtypes = [_vp]
@@ -573,6 +577,24 @@ def tune_dwt(filt, precision, log2n=24):
     ms = C.c_float()
     check(lib().wc_tune_dwt(filt, precision, log2n, C.byref(ms)))
     return get_dwt_tiling(filt, precision), ms.value
+
+
+def set_modwt_tiling(filt, precision, fwd_target, fwd_smem_kb, inv_target, inv_smem_kb):
+    check(lib().wc_set_modwt_tiling(filt, precision, fwd_target, fwd_smem_kb, inv_target,
+                                    inv_smem_kb))
+
+
+def get_modwt_tiling(filt, precision):
+    v = [C.c_int() for _ in range(4)]
+    check(lib().wc_get_modwt_tiling(filt, precision, *[C.byref(x) for x in v]))
+    return tuple(x.value for x in v)
+
+
+def tune_modwt(filt, precision, log2n=24, nlevels=12):
+    """Autotunes the MODWT tiling; returns (tiling, fwd_ms, inv_ms)."""
+    f, i = C.c_float(), C.c_float()
+    check(lib().wc_tune_modwt(filt, precision, log2n, nlevels, C.byref(f), C.byref(i)))
+    return get_modwt_tiling(filt, precision), f.value, i.value
 
 
 def device_count() -> int:

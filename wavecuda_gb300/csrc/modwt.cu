@@ -24,7 +24,9 @@
 // output is computed with the reference's term order, so WC_F64_EXACT stays
 // bit-identical however the levels are grouped.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
@@ -41,6 +43,13 @@ __device__ __forceinline__ void fwd_taps(const typename P::V* v, int stride, typ
   if constexpr (F == 1) {
     s = haar_sum<P>(v[0], v[stride]);
     d = haar_dif<P>(v[0], v[stride]);
+  } else if constexpr (std::is_same<P, PDD>::value) {
+    // d in lane 0, s in lane 1: the same operations as below, packed.
+    constexpr int L = filter_len(F);
+    dd_acc2 A = acc2_init(v[0], make_tap2(tap_g(F, 0), tap_h(F, 0)));
+#pragma unroll
+    for (int k = 1; k < L; k++) A = acc2_add(A, v[k * stride], make_tap2(tap_g(F, k), tap_h(F, k)));
+    acc2_fin(A, d, s);
   } else {
     constexpr int L = filter_len(F);
     typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
@@ -195,22 +204,59 @@ struct Geo {
   size_t smem;
 };
 
-constexpr size_t kTileSmem = 96 * 1024;
+// Tile configuration per (filter, precision): the values a tile aims at
+// (C * M) and the shared-memory budget per CTA, separately for the forward
+// and inverse kernels.  Defaults below; wc_tune_modwt() replaces them with
+// the fastest measured candidates.
+struct ModCfg {
+  int fwd_target, fwd_smem_kb, inv_target, inv_smem_kb;
+};
+
+std::mutex g_mcfg_mu;
+ModCfg g_mcfg[5][3];
+bool g_mcfg_set[5][3] = {};
+
+ModCfg default_mod_cfg(int prec) {
+  const int t = (prec == WC_F32) ? 4096 : 2048;
+  return ModCfg{t, 96, t, 96};
+}
+
+ModCfg get_mod_cfg(int F, int prec) {
+  std::lock_guard<std::mutex> lk(g_mcfg_mu);
+  if (!g_mcfg_set[F][prec]) {
+    g_mcfg[F][prec] = default_mod_cfg(prec);
+    g_mcfg_set[F][prec] = true;
+  }
+  return g_mcfg[F][prec];
+}
+
+void set_mod_cfg(int F, int prec, ModCfg c) {
+  std::lock_guard<std::mutex> lk(g_mcfg_mu);
+  g_mcfg[F][prec] = c;
+  g_mcfg_set[F][prec] = true;
+}
+
+template <class P>
+constexpr int prec_of() {
+  return std::is_same<P, PExact>::value ? WC_F64_EXACT
+         : std::is_same<P, PDD>::value  ? WC_F64_FAST
+                                        : WC_F32;
+}
 
 // Tile shape for level unit d0: C = min(d0, 32) columns and the largest
 // power-of-two row count M <= nrows with C*M <= target whose shared memory
 // fits the budget.
 template <class P>
-Geo<P> tile_geo(int64_t n, int l0, int halo, int arrays, int lead_rows) {
+Geo<P> tile_geo(int64_t n, int l0, int halo, int arrays, int lead_rows, int target,
+                size_t budget) {
   using V = typename P::V;
   const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
   const int C = (int)std::min<int64_t>(d0, 32);
-  const int target = (sizeof(V) == 4) ? 4096 : 2048;
   int M = (int)std::min<int64_t>(nrows, std::max(1, target / C));
   auto bytes = [&](int m) {
     return sizeof(V) * (size_t)C * (size_t)((m + halo) * arrays + lead_rows);
   };
-  while (M > 1 && bytes(M) > kTileSmem) M >>= 1;
+  while (M > 1 && bytes(M) > budget) M >>= 1;
   return {C, M, bytes(M)};
 }
 
@@ -222,11 +268,13 @@ int launch_fwd(const typename P::T* X, typename P::T* xmod, int64_t n, int l0, c
   constexpr int L = filter_len(F);
   constexpr int HR = (L - 1) * ((1 << NF) - 1);
   // In: M + HR rows; S1 (NF == 2): M + 2(L-1) rows.
-  Geo<P> g = tile_geo<P>(n, l0, HR, 1, NF == 2 ? 0 : 0);
+  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+  const size_t budget = (size_t)mc.fwd_smem_kb * 1024;
+  Geo<P> g = tile_geo<P>(n, l0, HR, 1, 0, mc.fwd_target, budget);
   if (NF == 2) {
     // recompute with both arrays
     using V = typename P::V;
-    while (g.M > 1 && sizeof(V) * (size_t)g.C * (size_t)((g.M + HR) + (g.M + 2 * (L - 1))) > kTileSmem)
+    while (g.M > 1 && sizeof(V) * (size_t)g.C * (size_t)((g.M + HR) + (g.M + 2 * (L - 1))) > budget)
       g.M >>= 1;
     g.smem = sizeof(V) * (size_t)g.C * (size_t)((g.M + HR) + (g.M + 2 * (L - 1)));
   }
@@ -245,8 +293,10 @@ int launch_inv(const typename P::T* Stop, const typename P::T* xmod, typename P:
                int64_t n, int l0, cudaStream_t s) {
   constexpr int L = filter_len(F);
   constexpr int HR = (L - 1) * ((1 << NI) - 1);
-  const int arrays = 1 + NI + (NI > 1 ? 2 : 0);
-  Geo<P> g = tile_geo<P>(n, l0, HR, arrays, 0);
+  // Stop tile, NI detail tiles and NI - 1 intermediates.
+  const int arrays = 2 * NI;
+  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+  Geo<P> g = tile_geo<P>(n, l0, HR, arrays, 0, mc.inv_target, (size_t)mc.inv_smem_kb * 1024);
   auto kern = modwt_inv_tiled<F, P, NI>;
   WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
   const int64_t blocks = (((int64_t)1 << l0) / g.C) * ((n >> l0) / g.M);
@@ -316,3 +366,124 @@ int modwt(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec, cud
 }
 
 }  // namespace wc
+
+// ---------------------------------------------------------------- tiling --
+
+namespace wc {
+namespace {
+
+int check_mod_cfg(int F, int prec, const ModCfg& c) {
+  if (F < 1 || F > 4 || prec < 0 || prec > 2) return fail(WC_ERR_ARG, "bad filter/precision");
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (!pow2(c.fwd_target) || !pow2(c.inv_target) || c.fwd_target < 256 || c.inv_target < 256 ||
+      c.fwd_target > 16384 || c.inv_target > 16384)
+    return fail(WC_ERR_ARG, "tile targets must be powers of two in [256, 16384]");
+  if (c.fwd_smem_kb < 16 || c.inv_smem_kb < 16 || c.fwd_smem_kb > 200 || c.inv_smem_kb > 200)
+    return fail(WC_ERR_ARG, "shared-memory budgets must lie in [16, 200] KB");
+  return WC_OK;
+}
+
+}  // namespace
+}  // namespace wc
+
+extern "C" int wc_set_modwt_tiling(int filter, int precision, int fwd_target, int fwd_smem_kb,
+                                   int inv_target, int inv_smem_kb) {
+  using namespace wc;
+  clear_error();
+  const ModCfg c{fwd_target, fwd_smem_kb, inv_target, inv_smem_kb};
+  WC_TRY(check_mod_cfg(filter, precision, c));
+  set_mod_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_get_modwt_tiling(int filter, int precision, int* fwd_target, int* fwd_smem_kb,
+                                   int* inv_target, int* inv_smem_kb) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  const ModCfg c = get_mod_cfg(filter, precision);
+  if (fwd_target) *fwd_target = c.fwd_target;
+  if (fwd_smem_kb) *fwd_smem_kb = c.fwd_smem_kb;
+  if (inv_target) *inv_target = c.inv_target;
+  if (inv_smem_kb) *inv_smem_kb = c.inv_smem_kb;
+  return WC_OK;
+}
+
+// Times the forward and the inverse MODWT (nlevels levels) of a 2^log2n
+// signal for each candidate tile target and shared-memory budget, and keeps
+// the fastest of each direction.
+extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, float* fwd_ms,
+                             float* inv_ms) {
+  using namespace wc;
+  clear_error();
+  WC_TRY(ensure_device());
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  if (log2n < 14 || log2n > 26) return fail(WC_ERR_ARG, "log2n must lie in [14, 26]");
+  const int64_t n = (int64_t)1 << log2n;
+  const int J = check_levels(n, nlevels, filter_len(filter));
+  if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid", nlevels);
+  const size_t es = (precision == WC_F32) ? 4 : 8;
+  void* x = nullptr;
+  void* xm = nullptr;
+  WC_CUDA(cudaMalloc(&x, es * (size_t)n));
+  if (cudaMalloc(&xm, es * (size_t)n * 2 * (size_t)J) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(x);
+    return fail(WC_ERR_NOMEM, "tuning buffers");
+  }
+  cudaStream_t s = lib_stream();
+  cudaMemsetAsync(x, 0x3c, es * (size_t)n, s);
+  const ModCfg keep = get_mod_cfg(filter, precision);
+  const int base = (precision == WC_F32) ? 2048 : 1024;
+  std::vector<std::pair<int, int>> cand;
+  for (int t : {base, 2 * base, 4 * base})
+    for (int kb : {48, 72, 96}) cand.push_back({t, kb});
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  float bf = 1e30f, bi = 1e30f;
+  ModCfg best = keep;
+  int rc = WC_OK;
+  for (const auto& c : cand) {
+    set_mod_cfg(filter, precision, ModCfg{c.first, c.second, c.first, c.second});
+    float mf = 1e30f, mi = 1e30f;
+    for (int rep = 0; rep < 3 && rc == WC_OK; rep++) {
+      cudaEventRecord(e0, s);
+      rc = modwt(x, xm, n, 1, J, filter, precision, s);
+      cudaEventRecord(e1, s);
+      if (rc == WC_OK) rc = modwt(x, xm, n, 0, J, filter, precision, s);
+      cudaEventRecord(e2, s);
+      cudaEventSynchronize(e2);
+      float a = 0.f, b = 0.f;
+      cudaEventElapsedTime(&a, e0, e1);
+      cudaEventElapsedTime(&b, e1, e2);
+      if (rep > 0) {
+        mf = std::min(mf, a);
+        mi = std::min(mi, b);
+      }
+    }
+    if (rc != WC_OK) break;
+    if (mf < bf) {
+      bf = mf;
+      best.fwd_target = c.first;
+      best.fwd_smem_kb = c.second;
+    }
+    if (mi < bi) {
+      bi = mi;
+      best.inv_target = c.first;
+      best.inv_smem_kb = c.second;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  cudaFree(x);
+  cudaFree(xm);
+  set_mod_cfg(filter, precision, rc == WC_OK ? best : keep);
+  if (fwd_ms) *fwd_ms = bf;
+  if (inv_ms) *inv_ms = bi;
+  return rc;
+}
