@@ -272,6 +272,12 @@ def ours(args):
             (tile, g0, th, pipe), tms = wc.tune_dwt(f, p, 24)
             tiling[f"{FILTERS[f]}/{PREC[p]}"] = {"tile": tile, "g0": g0, "threads": th,
                                                   "pipelined": pipe, "ms_2e24": round(tms, 4)}
+        if not args.no_sweep:
+            for f, p in sorted({(f, p) for f in (1, 2, 3, 4) for p in (0, 1, 2)}):
+                mt, fms, ims = wc.tune_modwt(f, p, 24, 12)
+                tiling[f"MODWT {FILTERS[f]}/{PREC[p]}"] = {
+                    "fwd_target": mt[0], "fwd_smem_kb": mt[1], "inv_target": mt[2],
+                    "inv_smem_kb": mt[3], "fwd_ms_2e24": round(fms, 4), "inv_ms_2e24": round(ims, 4)}
 
     clocks = ClockSampler()
     clocks.start()
@@ -378,12 +384,15 @@ def ours(args):
         out["sweep"] = sweep
     if tiling:
         out["tiling"] = tiling
-    if not args.no_batch:
-        out["batched"] = batch_bench(wc, args)
-    if not args.no_fit:
-        out["tuned"] = fit_bench(wc, args)
-    if not args.no_smooth:
-        out["smooth"] = smooth_bench(wc, args)
+    # Optional sections: a failure is recorded in the line, not fatal to it.
+    for key, skip, fn in (("batched", args.no_batch, batch_bench), ("tuned", args.no_fit, fit_bench),
+                          ("smooth", args.no_smooth, smooth_bench)):
+        if skip:
+            continue
+        try:
+            out[key] = fn(wc, args)
+        except Exception as e:  # noqa: BLE001 - reported in the JSON line
+            out[key] = {"error": f"{type(e).__name__}: {e}"}
     if dist.rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -498,7 +507,7 @@ def smooth_bench(wc, args):
                 ts.append(time.perf_counter() - t0)
                 mses.append(float(np.mean((y - f) ** 2)))
                 ths.append(info.thresh)
-                its.append(info.iterations)
+                its.append(info.cv_iterations)
             if prec == 0:
                 ref_t = ths
             out[f"{fname}/{PREC[prec]}"] = {
@@ -614,6 +623,13 @@ def profile_case(args):
     n = 1 << args.log2n
     x = np.random.default_rng(0).standard_normal(n)
     L = wc.lib()
+    if args.profile_case.startswith("batch:"):
+        # one persistent batched-smoothing launch over a 512-signal batch
+        prec = int(args.profile_case.split(":")[1])
+        data, sigs, _ = make_batch(wc, 512, seed=11)
+        wc.smooth_batch(data, sigs, prec)
+        print("ok", args.profile_case)
+        return
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
     es = 4 if prec == 2 else 8

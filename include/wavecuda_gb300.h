@@ -176,7 +176,8 @@ WC_API int wc_batch_plan_create(const wc_signal* signals, int nsig, int precisio
 WC_API int wc_batch_plan_destroy(wc_batch_plan plan);
 WC_API int wc_batch_plan_info(wc_batch_plan plan, int* grid, size_t* scratch_bytes);
 /* Times a few grid sizes on a scratch copy of data (device) and keeps the
- * fastest; data is not modified. */
+ * fastest; data is not modified.  Plans created later in the process (and
+ * wc_smooth_batch) start from the grid found, for the same precision. */
 WC_API int wc_batch_autotune(wc_batch_plan plan, const double* data, float* best_ms);
 /* Smooths every signal of data (device, FP64) in place: one CUDA-graph launch
  * of the queue reset and the persistent kernel, asynchronous on stream. */

@@ -499,6 +499,7 @@ __device__ __forceinline__ void q_of(double v, int eb_m, long long& q, bool& bad
 }
 
 struct SumShared {
+  float red_hi[32], red_lo[32];  // per-warp double-float partial sums
   long long warp_tot[32];
   unsigned long long mb;
   long long add;
@@ -597,6 +598,97 @@ __device__ void bcv_terms(const Y* ye, const Y* yo, const double* xn, int64_t le
     terms[j] = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
   }
   __syncthreads();
+}
+
+// |v| < t for t >= 0 and v not NaN, by comparing the magnitude bits as
+// unsigned integers (the same answer as the floating-point compare, without
+// an FP64 instruction).
+__device__ __forceinline__ bool abs_less(double v, double t) {
+  return ((unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull) <
+         (unsigned long long)__double_as_longlong(t);
+}
+__device__ __forceinline__ bool abs_less(float v, float t) {
+  return (__float_as_uint(v) & 0x7FFFFFFFu) < __float_as_uint(t);
+}
+
+// Double-float values of the working types (exact for float and dd).
+template <class V>
+__device__ __forceinline__ dd as_dd(V v) {
+  if constexpr (std::is_same<V, dd>::value) return v;
+  else return dd{(float)v, 0.f};
+}
+
+__device__ __forceinline__ dd dd_sqr(dd a) {
+  const float p = __fmul_rn(a.hi, a.hi);
+  float e = __fmaf_rn(a.hi, a.hi, -p);
+  e = __fmaf_rn(2.f * a.hi, a.lo, e);
+  dd r;
+  fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+
+// Sum over the block of one double-float value per thread; the FP64 result
+// is valid in every thread.
+__device__ double bdd_reduce(dd v, SumShared& sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const dd w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+    v = PDD::add(v, w);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    sh.red_hi[warp] = v.hi;
+    sh.red_lo[warp] = v.lo;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dd t{0.f, 0.f};
+    for (int w = 0; w < nw; w++) t = PDD::add(t, dd{sh.red_hi[w], sh.red_lo[w]});
+    sh.red_hi[0] = t.hi;
+    sh.red_lo[0] = t.lo;
+  }
+  __syncthreads();
+  const double r = dd_to_double(dd{sh.red_hi[0], sh.red_lo[0]});
+  __syncthreads();
+  return r;
+}
+
+// Sum of the interpolation loss terms (the quantity bcv_terms + bseq_sum
+// give).  Exact FP64: the reference's roundings and serial order.  The other
+// precisions already differ from the reference in the reconstructions, so
+// there the terms and their sum run in double-float on the FP32 pipes
+// (GB300's FP64 pipe is about 1/64 of its FP32 rate), in block order.
+template <class P>
+__device__ double bcv_sum(const typename P::V* ye, const typename P::V* yo, const double* xn,
+                          int64_t lenh, double* terms, SumShared& sh) {
+  using V = typename P::V;
+  if constexpr (std::is_same<P, PExact>::value) {
+    bcv_terms<V>(ye, yo, xn, lenh, terms);
+    return bseq_sum(terms, lenh, sh);
+  } else {
+    const dd half{0.5f, 0.f};
+    dd acc{0.f, 0.f};
+    for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
+      dd yie, yio;
+      if (j == 0) {
+        yie = as_dd(yo[0]);
+        yio = PDD::add(as_dd(ye[0]), as_dd(ye[1]));
+        yio = dd{yio.hi * half.hi, yio.lo * half.hi};
+      } else if (j == lenh - 1) {
+        yio = as_dd(ye[lenh - 1]);
+        yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
+        yie = dd{yie.hi * half.hi, yie.lo * half.hi};
+      } else {
+        yio = PDD::add(as_dd(ye[j]), as_dd(ye[j + 1]));
+        yio = dd{yio.hi * half.hi, yio.lo * half.hi};
+        yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
+        yie = dd{yie.hi * half.hi, yie.lo * half.hi};
+      }
+      const dd a = PDD::sub(yie, dd_from_double(xn[2 * j]));
+      const dd b = PDD::sub(yio, dd_from_double(xn[2 * j + 1]));
+      acc = PDD::add(acc, PDD::add(dd_sqr(a), dd_sqr(b)));
+    }
+    return bdd_reduce(acc, sh);
+  }
 }
 
 // ------------------------------------------------------------ pipeline --
@@ -758,10 +850,8 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
     step(1, t1);
     step(2, t2);
     step(3, t2);
-    bcv_terms<V>(y[0], y[1], x, lenh, terms);
-    double m1 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
-    bcv_terms<V>(y[2], y[3], x, lenh, terms);
-    double m2 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+    double m1 = __dmul_rn(bcv_sum<P>(y[0], y[1], x, lenh, terms, sh.sum), 0.5);
+    double m2 = __dmul_rn(bcv_sum<P>(y[2], y[3], x, lenh, terms, sh.sum), 0.5);
     while (fabs(__dsub_rn(t3, t0)) > __dmul_rn(d.tol, __dadd_rn(t1, t2))) {
       if (iters > 50) break;
       if (m1 != 0.0) min_margin = fmin(min_margin, fabs(__dsub_rn(m1, m2)) / fabs(m1));
@@ -770,15 +860,13 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
         m1 = m2;
         step(2, t2);
         step(3, t2);
-        bcv_terms<V>(y[2], y[3], x, lenh, terms);
-        m2 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+        m2 = __dmul_rn(bcv_sum<P>(y[2], y[3], x, lenh, terms, sh.sum), 0.5);
       } else {
         t3 = t2; t2 = t1; t1 = __dadd_rn(__dmul_rn(R, t1), __dmul_rn(C, t0));
         m2 = m1;
         step(0, t1);
         step(1, t1);
-        bcv_terms<V>(y[0], y[1], x, lenh, terms);
-        m1 = __dmul_rn(bseq_sum(terms, lenh, sh.sum), 0.5);
+        m1 = __dmul_rn(bcv_sum<P>(y[0], y[1], x, lenh, terms, sh.sum), 0.5);
       }
       iters++;
     }
@@ -797,15 +885,16 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
     if (threadIdx.x == 0) cnt[0] = cnt[1] = 0;
     __syncthreads();
     unsigned long long k0 = 0, z0 = 0;
+    const T t_cmp = (T)t;
     if (!mod) {
       for (int64_t i = 1 + threadIdx.x; i < n; i += blockDim.x) {
         const int l = __ffsll((long long)i) - 1;
         if (l >= J || l < d.minl || l > d.maxl) continue;
-        if (fabs((double)w[i]) < t) z0++; else k0++;
+        if (abs_less(w[i], t_cmp)) z0++; else k0++;
       }
     } else {
       for (int64_t e = threadIdx.x; e < (int64_t)(d.maxl - d.minl + 1) * n; e += blockDim.x) {
-        if (fabs((double)w[(int64_t)d.minl * n + e]) < t) z0++; else k0++;
+        if (abs_less(w[(int64_t)d.minl * n + e], t_cmp)) z0++; else k0++;
       }
     }
     atomicAdd(&cnt[0], k0);

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -51,6 +52,10 @@ void free_plan(wc_batch_plan_s* p) {
   cudaFree(p->d_scratch);
   delete p;
 }
+
+// Grid chosen by the last wc_batch_autotune per precision (0: none yet);
+// later plans of the process start from it.
+std::atomic<int> g_tuned_grid[3];
 
 int launch_direct(wc_batch_plan_s* p, double* data, int grid, cudaStream_t s) {
   WC_CUDA(cudaMemsetAsync(p->d_counter, 0, sizeof(int), s));
@@ -121,6 +126,7 @@ int wc_batch_plan_create(const wc_signal* sigs, int nsig, int precision, wc_batc
   size_t freeb = 0, totb = 0;
   cudaMemGetInfo(&freeb, &totb);
   int grid = batch_max_ctas(precision);
+  if (g_tuned_grid[precision].load() > 0) grid = std::min(grid, g_tuned_grid[precision].load());
   const size_t cap = (freeb / 2) / std::max<size_t>(p->scratch_per_cta, 1);
   grid = (int)std::min<size_t>((size_t)grid, std::max<size_t>(cap, 1));
   grid = std::min(grid, nsig);
@@ -252,6 +258,7 @@ int wc_batch_autotune(wc_batch_plan plan, const double* data, float* best_ms) {
   cudaFree(copy);
   if (rc != WC_OK) return rc;
   plan->grid = best_g;
+  g_tuned_grid[plan->prec].store(best_g);
   if (best_ms) *best_ms = best;
   return WC_OK;
 }
