@@ -17,7 +17,7 @@
  * Codes (wvtheads.h:14-38, rfunctions.cuh:13-15 of the reference):
  *   sense     FWD 1, BWD 0
  *   filter    HAAR 1, D4 2, C6 3, LA8 4          (filterlen 2, 4, 6, 8)
- *   ttype     DWT 0, MODWT (time ordered) 1
+ *   ttype     DWT 0, MODWT (time ordered) 1, MODWT (packet ordered) 2
  *   hardness  HARD 0, SOFT 1
  *   threshtype MANUAL 0, UNIV 1, CV 2
  *   levels are 0-based in C (R's min.level - 1).
@@ -27,6 +27,12 @@
  *         level-l details (1-based) sit at indices = 2^(l-1) mod 2^l and the
  *         level-J scaling coefficients at indices = 0 mod 2^J.
  *   MODWT xmod = [s_1 | d_1 | s_2 | d_2 | ... | s_J | d_J], 2*len*J values.
+ *   MODWT packet ordered (haar.cpp:305-398, daub4.cpp:392-484): level block
+ *         l (2*len values) holds 2^(l+1) packets; packet sh has the (s, d)
+ *         pairs of time positions rev(sh, l+1) + 2^(l+1) k, interleaved
+ *         (convert_modwt_level, wavutils.cpp:569-600).  The transform, host
+ *         thresholding and smoothing calls accept it; the batched, tuning and
+ *         device-pointer MODWT calls take time order.
  *
  * Precision codes (wc_* calls; the R symbols use the process default):
  *   WC_F64_EXACT  FP64, every product and sum rounded in the reference's order

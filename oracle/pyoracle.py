@@ -25,7 +25,7 @@ REF_SO = os.path.join(HERE, "_ref", "libwavref.so")
 
 HAAR, D4, C6, LA8 = 1, 2, 3, 4
 FILTER_LEN = {HAAR: 2, D4: 4, C6: 6, LA8: 8}
-DWT, MODWT = 0, 1
+DWT, MODWT, MODWT_PO = 0, 1, 2
 FWD, BWD = 1, 0
 HARD, SOFT = 0, 1
 MANUAL, UNIV, CV = 0, 1, 2
@@ -89,6 +89,7 @@ class Oracle:
                                 C.c_int, C.c_int, C.c_int, C.c_double]
         L.wo_count_kept.argtypes = [_dp, _dp, _i64, C.c_int, C.c_int, C.c_double,
                                     C.c_int, C.c_int, C.POINTER(_i64), C.POINTER(_i64)]
+        L.wo_modwt_po.argtypes = [_dp, _dp, _i64, C.c_int, C.c_int, C.c_int]
         L.wo_set_threads.argtypes = [C.c_int]
         L.wo_get_threads.restype = C.c_int
 
@@ -115,6 +116,21 @@ class Oracle:
         if self.lib.wo_modwt(_ptr(x), _ptr(xmod), x.size, FWD, J, filt):
             raise ValueError("oracle modwt rejected the arguments")
         return xmod
+
+    def modwt_po_fwd(self, x, nlevels, filt):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        J = self.levels(x.size, nlevels, filt)
+        xmod = np.zeros(2 * J * x.size)
+        if self.lib.wo_modwt_po(_ptr(x), _ptr(xmod), x.size, FWD, J, filt):
+            raise ValueError("oracle modwt_po rejected the arguments")
+        return xmod
+
+    def modwt_po_inv(self, xmod, n, nlevels, filt):
+        xm = np.array(xmod, dtype=np.float64, copy=True)
+        x = np.zeros(n)
+        if self.lib.wo_modwt_po(_ptr(x), _ptr(xm), n, BWD, nlevels, filt):
+            raise ValueError("oracle modwt_po rejected the arguments")
+        return x
 
     def modwt_inv(self, xmod, n, nlevels, filt):
         xm = np.array(xmod, dtype=np.float64, copy=True)
@@ -224,6 +240,23 @@ class Reference:
         r = self.lib.wref_transform(_ptr(x), _ptr(xm), n, BWD, nlevels, MODWT, filt,
                                     FILTER_LEN[filt])
         if r:
+            raise ValueError("reference transform failed")
+        return x
+
+    def modwt_po_fwd(self, x, nlevels, filt):
+        x = np.array(x, dtype=np.float64, copy=True)
+        J = self.levels(x.size, nlevels, filt)
+        xmod = np.zeros(2 * J * x.size)
+        if self.lib.wref_transform(_ptr(x), _ptr(xmod), x.size, FWD, J, MODWT_PO, filt,
+                                   FILTER_LEN[filt]):
+            raise ValueError("reference transform failed")
+        return xmod
+
+    def modwt_po_inv(self, xmod, n, nlevels, filt):
+        xm = np.array(xmod, dtype=np.float64, copy=True)
+        x = np.zeros(n)
+        if self.lib.wref_transform(_ptr(x), _ptr(xm), n, BWD, nlevels, MODWT_PO, filt,
+                                   FILTER_LEN[filt]):
             raise ValueError("reference transform failed")
         return x
 

@@ -35,6 +35,7 @@
 #define WO_LA8 4
 #define WO_DWT 0
 #define WO_MODWT 1
+#define WO_MODWT_PO 2
 #define WO_HARD 0
 #define WO_SOFT 1
 
@@ -305,6 +306,122 @@ int wo_modwt(double* x, double* xmod, int64_t len, int sense, int nlevels,
   return 0;
 }
 
+/* ------------------------------------------------- packet-ordered MODWT -- */
+
+/* Reverses the low nb bits of v (reverse_bits, utils.cpp:254). */
+static int64_t rev_bits(int64_t v, int nb) {
+  int64_t r = 0;
+  for (int i = 0; i < nb; i++) r = (r << 1) | ((v >> i) & 1);
+  return r;
+}
+
+/* Level l of the packet-ordered layout from the time-ordered one
+ * (convert_modwt_level, wavutils.cpp:569-600): packet `sh` holds the (s, d)
+ * pairs of time positions t = rev(sh, l+1) + 2^(l+1) k, interleaved. */
+static void to_to_po_level(const double* to, double* po, int64_t len, int l) {
+  const int64_t skip = (int64_t)1 << l, lenos = len / skip, np = 2 * skip;
+  for (int64_t sh = 0; sh < np; sh++) {
+    const int64_t st = rev_bits(sh, l + 1);
+    for (int64_t k = 0; k < lenos / 2; k++) {
+      po[sh * lenos + 2 * k] = to[st + 2 * skip * k];
+      po[sh * lenos + 2 * k + 1] = to[len + st + 2 * skip * k];
+    }
+  }
+}
+
+static void po_to_to_level(const double* po, double* to, int64_t len, int l) {
+  const int64_t skip = (int64_t)1 << l, lenos = len / skip, np = 2 * skip;
+  for (int64_t sh = 0; sh < np; sh++) {
+    const int64_t st = rev_bits(sh, l + 1);
+    for (int64_t k = 0; k < lenos / 2; k++) {
+      to[st + 2 * skip * k] = po[sh * lenos + 2 * k];
+      to[len + st + 2 * skip * k] = po[sh * lenos + 2 * k + 1];
+    }
+  }
+}
+
+/* One value of the one-level inverse DWT of a packet (bHaar / bDaub4 / ...
+ * on lenos values, as dwt_inv_level) at packet position i; the packet's
+ * pairs are (S, D)[r + 2 skip q], q < P. */
+static double po_packet_inv(const double* S, const double* D, int64_t r, int64_t skip,
+                            int64_t P, int64_t i, int filter, const double* h,
+                            const double* g) {
+  const int64_t q = i >> 1;
+  const int odd = (int)(i & 1);
+  if (filter == WO_HAAR) {
+    const double a = S[r + 2 * skip * q], b = D[r + 2 * skip * q];
+    return odd ? (a - b) * kInvR2 : (a + b) * kInvR2;
+  }
+  const int H = wo_filter_length(filter) / 2;
+  double acc = 0.0;
+  for (int j = H - 1; j >= 0; j--) {
+    const int64_t p = ((q - j) % P + P) % P;
+    const double sv = S[r + 2 * skip * p], dv = D[r + 2 * skip * p];
+    if (j == H - 1) acc = sv * h[2 * j + odd];
+    else acc = acc + sv * h[2 * j + odd];
+    acc = acc + dv * g[2 * j + odd];
+  }
+  return acc;
+}
+
+/* Inverse of level l (bHaarMODWT, haar.cpp:363-398; bDaub4MODWTpo,
+ * daub4.cpp:449-484): every packet pair (2m, 2m+1) is inverted one DWT level
+ * and the two reconstructions are averaged, writeavpackets
+ * (wavutils.cpp:304-330): out = 0.5 * (y_2m[i] + y_2m+1[(i - 1) mod lenos]).
+ * In time order, packet 2m has residue st = u mod skip and packet 2m+1
+ * residue st + skip (mod 2 skip); u = st + skip i. */
+static void po_inv_level(const double* S, const double* D, double* out, int64_t len, int l,
+                         int filter) {
+  double h[8], g[8];
+  get_taps(filter, h, g);
+  const int64_t skip = (int64_t)1 << l, lenos = len / skip, P = lenos / 2;
+  for (int64_t u = 0; u < len; u++) {
+    const int64_t st = u % skip, i = u / skip;
+    const double a = po_packet_inv(S, D, st, skip, P, i, filter, h, g);
+    const double b = po_packet_inv(S, D, st + skip, skip, P, (i + lenos - 1) % lenos, filter,
+                                   h, g);
+    out[u] = 0.5 * (a + b);
+  }
+}
+
+int wo_modwt_po(double* x, double* xmod, int64_t len, int sense, int nlevels, int filter) {
+  int L = wo_filter_length(filter);
+  if (L == 0) return 1;
+  int J = wo_check_len_levels(len, nlevels, L);
+  if (J == 0) return 1;
+  double* to = (double*)malloc(sizeof(double) * (size_t)(2 * (int64_t)J * len));
+  if (!to) return 1;
+  if (sense == WO_FWD) {
+    /* fHaarMODWT / fDaub4MODWTpo compute the same coefficients as the
+     * time-ordered transform, stored per packet. */
+    wo_modwt(x, to, len, WO_FWD, J, filter);
+    for (int l = 0; l < J; l++)
+      to_to_po_level(to + 2 * (int64_t)l * len, xmod + 2 * (int64_t)l * len, len, l);
+  } else if (sense == WO_BWD) {
+    for (int l = 0; l < J; l++)
+      po_to_to_level(xmod + 2 * (int64_t)l * len, to + 2 * (int64_t)l * len, len, l);
+    double* cur = (double*)malloc(sizeof(double) * (size_t)len);
+    double* nxt = (double*)malloc(sizeof(double) * (size_t)len);
+    if (!cur || !nxt) {
+      free(cur); free(nxt); free(to);
+      return 1;
+    }
+    memcpy(cur, to + 2 * (int64_t)(J - 1) * len, sizeof(double) * (size_t)len);
+    for (int l = J - 1; l >= 0; l--) {
+      double* dst = (l == 0) ? x : nxt;
+      po_inv_level(cur, to + (2 * (int64_t)l + 1) * len, dst, len, l, filter);
+      double* t = cur; cur = nxt; nxt = t;
+    }
+    free(cur);
+    free(nxt);
+  } else {
+    free(to);
+    return 1;
+  }
+  free(to);
+  return 0;
+}
+
 /* ----------------------------------------------------------- threshold -- */
 
 double wo_thresh_coef(double coef, double thresh, int hardness) {
@@ -352,6 +469,17 @@ static void threshold_modwt(const double* in, double* out, int64_t len,
   }
 }
 
+/* Packet order: the details sit at the odd indices of each level block
+ * (thresh.cpp:56-64). */
+static void threshold_modwt_po(double* xm, int64_t len, double thresh, int hardness,
+                               int minlevel, int maxlevel) {
+  for (int l = minlevel; l <= maxlevel; l++) {
+    int64_t il = (int64_t)2 * l * len;
+    for (int64_t i = 1; i < 2 * len; i += 2)
+      xm[il + i] = wo_thresh_coef(xm[il + i], thresh, hardness);
+  }
+}
+
 int wo_threshold(double* x, double* xmod, int64_t len, int nlevels, int ttype,
                  int filter, double thresh, int hardness, int minlevel,
                  int maxlevel) {
@@ -361,6 +489,8 @@ int wo_threshold(double* x, double* xmod, int64_t len, int nlevels, int ttype,
     threshold_dwt(x, NULL, len, thresh, hardness, minlevel, maxlevel, nlevels, 0);
   else if (ttype == WO_MODWT)
     threshold_modwt(xmod, NULL, len, thresh, hardness, minlevel, maxlevel, nlevels);
+  else if (ttype == WO_MODWT_PO)
+    threshold_modwt_po(xmod, len, thresh, hardness, minlevel, maxlevel);
   else
     return 1;
   return 0;

@@ -45,6 +45,10 @@ int wo_dwt(double* x, int64_t len, int sense, int nlevels, int filter);
 int wo_modwt(double* x, double* xmod, int64_t len, int sense, int nlevels,
              int filter);
 
+/* Packet-ordered MODWT (code 2; haar.cpp:305-398, daub4.cpp:392-484), any
+ * filter.  FWD: x -> xmod (2*len*J values, packet order).  BWD: xmod -> x. */
+int wo_modwt_po(double* x, double* xmod, int64_t len, int sense, int nlevels, int filter);
+
 /* thresh_coef (thresh.cpp:142-157). */
 double wo_thresh_coef(double coef, double thresh, int hardness);
 

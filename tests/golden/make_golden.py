@@ -90,6 +90,27 @@ def main():
         y, t = R.smooth(x, J, ttype, filt, tt[kind], 0.35, hard, mn, mx, 1e-8)
         put(f"smooth_{kind}_f{filt}_t{ttype}_h{hard}_{mn}_{mx}",
             [n, J, ttype, filt, tt[kind], hard, mn, mx], x, y, t)
+    # Packet-ordered MODWT (code 2; Haar and D4 only in the reference):
+    # transforms, and smoothing through RcpuSmooth with ttype 2.
+    rng_po = np.random.default_rng(30)
+    for filt in (P.HAAR, P.D4):
+        n = 256
+        for J in (1, 3, R.levels(n, 0, filt)):
+            x = rng_po.standard_normal(n)
+            xm = R.modwt_po_fwd(x, J, filt)
+            put(f"modwtpo_fwd_f{filt}_256_j{J}", [n, J, filt, P.FWD], x, xm)
+            put(f"modwtpo_inv_f{filt}_256_j{J}", [n, J, filt, P.BWD], xm,
+                R.modwt_po_inv(xm, n, J, filt))
+    po_cases = [("cv", P.HAAR, P.SOFT, 0, 9), ("cv", P.D4, P.SOFT, 0, 8),
+                ("cv", P.D4, P.HARD, 1, 7), ("univ", P.HAAR, P.HARD, 0, 9),
+                ("manual", P.D4, P.SOFT, 2, 8)]
+    for k, (kind, filt, hard, mn, mx) in enumerate(po_cases):
+        n = 1024
+        J = R.levels(n, 0, filt) if filt != P.HAAR else 10
+        x = signals.noisy(signals.doppler(n), 5.0, seed=300 + k)
+        y, t = R.smooth(x, J, P.MODWT_PO, filt, tt[kind], 0.35, hard, mn, mx, 1e-8)
+        put(f"smoothpo_{kind}_f{filt}_h{hard}_{mn}_{mx}",
+            [n, J, P.MODWT_PO, filt, tt[kind], hard, mn, mx], x, y, t)
     np.savez_compressed(OUT, **fx)
     print(f"wrote {len(fx)} arrays to {OUT} ({os.path.getsize(OUT)} bytes)")
 

@@ -66,3 +66,20 @@ def test_perfect_reconstruction_and_parseval(oracle, filt):
     assert np.max(np.abs(oracle.dwt(w, J, filt, P.BWD) - x)) < 1e-13
     xm = oracle.modwt_fwd(x, 6, filt)
     assert np.max(np.abs(oracle.modwt_inv(xm, 512, 6, filt) - x)) < 1e-13
+
+
+def test_golden_packet_ordered_modwt(oracle, golden):
+    """Packet-ordered MODWT (code 2): the oracle reproduces the reference's
+    fHaarMODWT / fDaub4MODWTpo and their inverses bit for bit."""
+    n_checked = 0
+    for name, f in golden.items():
+        if not name.startswith("modwtpo_"):
+            continue
+        n, J, filt, sense = (int(v) for v in f["args"])
+        if sense == P.FWD:
+            got = oracle.modwt_po_fwd(f["in"], J, filt)
+        else:
+            got = oracle.modwt_po_inv(f["in"], n, J, filt)
+        assert np.array_equal(got, f["out"]), name
+        n_checked += 1
+    assert n_checked == 12

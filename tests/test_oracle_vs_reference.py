@@ -54,3 +54,15 @@ def test_univ_thresh_levels(oracle, reference):
             for mx in range(mn, J):
                 assert oracle.univ_thresh(w, 512, J, ttype, mn, mx) == \
                     reference.univ_thresh(w, 512, J, ttype, filt, mn, mx)
+
+
+@pytest.mark.parametrize("filt", [P.HAAR, P.D4])
+def test_packet_ordered_modwt_bit_identical(oracle, reference, filt):
+    rng = np.random.default_rng(6)
+    for n in (8, 64, 1024):
+        for J in range(1, oracle.levels(n, 0, filt) + 1):
+            x = rng.standard_normal(n)
+            xm = reference.modwt_po_fwd(x, J, filt)
+            assert np.array_equal(oracle.modwt_po_fwd(x, J, filt), xm)
+            assert np.array_equal(oracle.modwt_po_inv(xm, n, J, filt),
+                                  reference.modwt_po_inv(xm, n, J, filt))

@@ -26,7 +26,7 @@ LIB_PATH = os.path.join(HERE, "libwavecuda_gb300.so")
 # Codes (wvtheads.h:14-38, rfunctions.cuh:13-15).
 FWD, BWD = 1, 0
 HAAR, D4, C6, LA8 = 1, 2, 3, 4
-DWT, MODWT = 0, 1
+DWT, MODWT, MODWT_PO = 0, 1, 2
 HARD, SOFT = 0, 1
 MANUAL, UNIV, CV = 0, 1, 2
 F64_EXACT, F64_FAST, F32 = 0, 1, 2

@@ -207,9 +207,10 @@ int default_prec() {
 
 int check_codes(int64_t len, int ttype, int filter, int sense_or_0) {
   if (filter < 1 || filter > 4) return fail(WC_ERR_ARG, "unrecognised filter %d", filter);
-  if (ttype != 0 && ttype != 1)
-    return fail(ttype == 2 ? WC_ERR_UNSUPPORTED : WC_ERR_ARG,
-                "transform type %d not provided (0 DWT, 1 time-ordered MODWT)", ttype);
+  if (ttype < 0 || ttype > 2)
+    return fail(WC_ERR_ARG,
+                "transform type %d not provided (0 DWT, 1 time-ordered MODWT, 2 packet-ordered MODWT)",
+                ttype);
   if (sense_or_0 != 0 && sense_or_0 != 1) return fail(WC_ERR_ARG, "sense must be 1 (FWD) or 0 (BWD)");
   if (len <= 0 || (len & (len - 1)) != 0) return fail(WC_ERR_ARG, "length %lld is not a power of 2", (long long)len);
   return WC_OK;
@@ -268,11 +269,11 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
   if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld and filter length %d",
                           nlevels, (long long)len, filterlen);
   if (prec < 0 || prec > 2) return fail(WC_ERR_ARG, "unknown precision %d", prec);
-  if (!x || (ttype == 1 && !xmod)) return fail(WC_ERR_ARG, "null data pointer");
+  if (!x || (ttype != 0 && !xmod)) return fail(WC_ERR_ARG, "null data pointer");
   cudaStream_t s = lib_stream();
-  const int64_t nx = len, nm = (ttype == 1) ? 2 * len * (int64_t)J : 0;
+  const int64_t nx = len, nm = (ttype != 0) ? 2 * len * (int64_t)J : 0;
   const size_t bx = sizeof(double) * (size_t)nx, bm = sizeof(double) * (size_t)nm;
-  double* A = static_cast<double*>(workspace(kSlotStageA, ttype == 1 ? bm : bx));
+  double* A = static_cast<double*>(workspace(kSlotStageA, ttype != 0 ? bm : bx));
   double* B = static_cast<double*>(workspace(kSlotStageB, bx));
   if (!A || !B) return workspace_error();
   float* fa = nullptr;
@@ -280,7 +281,7 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
   if (prec == WC_F32) {
     // fa: the transform's FP32 input or output (nm values for MODWT, nx for
     // DWT); fb: the FP32 signal (nx values).  Both carved from one slot.
-    const size_t abytes = ((sizeof(float) * (size_t)(ttype == 1 ? nm : nx) + 255) / 256) * 256;
+    const size_t abytes = ((sizeof(float) * (size_t)(ttype != 0 ? nm : nx) + 255) / 256) * 256;
     const size_t bbytes = ((sizeof(float) * (size_t)nx + 255) / 256) * 256;
     char* f = static_cast<char*>(workspace(kSlotConvert, abytes + bbytes));
     if (!f) return workspace_error();
@@ -305,26 +306,33 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
       WC_TRY(dwt(A, B, len, sense, J, filter, prec, s));
     }
     WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
-  } else if (sense == 1) {
-    WC_CUDA(cudaMemcpyAsync(B, x, bx, cudaMemcpyHostToDevice, s));
-    if (prec == WC_F32) {
-      WC_TRY(convert(B, fb, nx, s));
-      WC_TRY(modwt(fb, fa, len, 1, J, filter, prec, s));
-      WC_TRY(convert(fa, A, nm, s));
-    } else {
-      WC_TRY(modwt(B, A, len, 1, J, filter, prec, s));
-    }
-    WC_CUDA(cudaMemcpyAsync(xmod, A, bm, cudaMemcpyDeviceToHost, s));
   } else {
-    WC_CUDA(cudaMemcpyAsync(A, xmod, bm, cudaMemcpyHostToDevice, s));
-    if (prec == WC_F32) {
-      WC_TRY(convert(A, fa, nm, s));
-      WC_TRY(modwt(fb, fa, len, 0, J, filter, prec, s));
-      WC_TRY(convert(fb, B, nx, s));
+    // time order (ttype 1) or packet order (ttype 2, modwt_po)
+    auto mod = [&](void* xs, void* xm, int sn) {
+      return ttype == 2 ? modwt_po(xs, xm, len, sn, J, filter, prec, s)
+                        : modwt(xs, xm, len, sn, J, filter, prec, s);
+    };
+    if (sense == 1) {
+      WC_CUDA(cudaMemcpyAsync(B, x, bx, cudaMemcpyHostToDevice, s));
+      if (prec == WC_F32) {
+        WC_TRY(convert(B, fb, nx, s));
+        WC_TRY(mod(fb, fa, 1));
+        WC_TRY(convert(fa, A, nm, s));
+      } else {
+        WC_TRY(mod(B, A, 1));
+      }
+      WC_CUDA(cudaMemcpyAsync(xmod, A, bm, cudaMemcpyDeviceToHost, s));
     } else {
-      WC_TRY(modwt(B, A, len, 0, J, filter, prec, s));
+      WC_CUDA(cudaMemcpyAsync(A, xmod, bm, cudaMemcpyHostToDevice, s));
+      if (prec == WC_F32) {
+        WC_TRY(convert(A, fa, nm, s));
+        WC_TRY(mod(fb, fa, 0));
+        WC_TRY(convert(fb, B, nx, s));
+      } else {
+        WC_TRY(mod(B, A, 0));
+      }
+      WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
     }
-    WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
   }
   WC_CUDA(cudaStreamSynchronize(s));
   return WC_OK;
@@ -349,7 +357,16 @@ int threshold_host(double* x, double* xmod, int64_t len, int nlevels, int ttype,
   double* A = static_cast<double*>(workspace(kSlotStageA, b));
   if (!A) return workspace_error();
   WC_CUDA(cudaMemcpyAsync(A, data, b, cudaMemcpyHostToDevice, s));
-  WC_TRY(wc::threshold(A, len, J, ttype, t, hardness, minl, maxl, WC_F64_EXACT, s));
+  if (ttype == 2) {
+    // packet order: the same coefficients permuted, so threshold in time order
+    double* T = static_cast<double*>(workspace(kSlotPacket, b));
+    if (!T) return workspace_error();
+    WC_TRY(modwt_layout(A, T, len, J, 0, WC_F64_EXACT, s));
+    WC_TRY(wc::threshold(T, len, J, 1, t, hardness, minl, maxl, WC_F64_EXACT, s));
+    WC_TRY(modwt_layout(T, A, len, J, 1, WC_F64_EXACT, s));
+  } else {
+    WC_TRY(wc::threshold(A, len, J, ttype, t, hardness, minl, maxl, WC_F64_EXACT, s));
+  }
   WC_CUDA(cudaMemcpyAsync(data, A, b, cudaMemcpyDeviceToHost, s));
   WC_CUDA(cudaStreamSynchronize(s));
   return WC_OK;

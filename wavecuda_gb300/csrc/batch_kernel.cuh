@@ -114,6 +114,26 @@ __device__ __forceinline__ double to_d(V v) {
   else return (double)v;
 }
 
+// Outputs per thread per sweep of the block-level transform loops: the taps of
+// U outputs are loaded before any is combined, so that U * L independent
+// loads are in flight per thread (the sequences live in global memory).
+// Full sweeps of U outputs carry no bounds checks; the remainder runs one
+// output at a time.  FP32 takes 4 outputs; the 8-byte value types (FP64,
+// double-float) are arithmetic-bound and keep one (measured: two outputs
+// per thread slowed the double-float batch by 30 %).
+template <class V>
+constexpr int mod_unroll() {
+  return sizeof(V) == 4 ? 4 : 1;
+}
+
+template <int U, class Fn>
+__device__ __forceinline__ void sweep_outputs(int64_t N, Fn fn) {
+  const int64_t B = blockDim.x, step = U * B, full = (N / step) * step;
+  int64_t i0 = threadIdx.x;
+  for (; i0 < full; i0 += step) fn(std::integral_constant<int, U>{}, i0);
+  for (; i0 < N; i0 += B) fn(std::integral_constant<int, 1>{}, i0);
+}
+
 // ------------------------------------------------------- DWT (block) ----
 
 // Forward DWT of y (compact, N values, type S) into the interleaved T array
@@ -184,48 +204,59 @@ __device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_
     const V* s = (l & 1) ? tB : tA;   // level l+1 values (Nl of them)
     V* dstv = (l & 1) ? tA : tB;
     const int64_t off = (int64_t)1 << l, step = (int64_t)2 << l;
-    for (int64_t q = threadIdx.x; q < Nl; q += blockDim.x) {
-      V e, o;
-      if constexpr (F == 1) {
-        const V sv = s[q];
-        const V dv = thr_v<P>(P::ld(w[off + q * step]), th, l);
-        e = haar_sum<P>(sv, dv);
-        o = haar_dif<P>(sv, dv);
-      } else {
-        V sv[H], dv[H];
+    const int64_t B = blockDim.x;
+    sweep_outputs<mod_unroll<V>()>(Nl, [&](auto uc, int64_t q0) {
+      constexpr int UU = decltype(uc)::value;
+      V sv[UU][H], dv[UU][H];
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
 #pragma unroll
         for (int j = 0; j < H; j++) {
-          const int64_t p = (q - j) & (Nl - 1);
-          sv[j] = s[p];
-          dv[j] = thr_v<P>(P::ld(w[off + p * step]), th, l);
+          const int64_t p = (q0 + u * B - j) & (Nl - 1);
+          sv[u][j] = s[p];
+          dv[u][j] = P::ld(w[off + p * step]);
         }
-        typename P::Acc ae = P::acc_init(sv[H - 1], tap_h(F, 2 * (H - 1)));
-        typename P::Acc ao = P::acc_init(sv[H - 1], tap_h(F, 2 * (H - 1) + 1));
-        ae = P::acc_add(ae, dv[H - 1], tap_g(F, 2 * (H - 1)));
-        ao = P::acc_add(ao, dv[H - 1], tap_g(F, 2 * (H - 1) + 1));
+      }
 #pragma unroll
-        for (int j = H - 2; j >= 0; j--) {
-          ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
-          ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
-          ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
-          ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
-        }
-        e = P::acc_fin(ae);
-        o = P::acc_fin(ao);
-      }
-      if (l == 0) {
-        if constexpr (std::is_same<D, typename P::V>::value) {
-          out[2 * q] = e;
-          out[2 * q + 1] = o;
+      for (int u = 0; u < UU; u++) {
+        const int64_t q = q0 + u * B;
+        V e, o;
+        if constexpr (F == 1) {
+          const V dq = thr_v<P>(dv[u][0], th, l);
+          e = haar_sum<P>(sv[u][0], dq);
+          o = haar_dif<P>(sv[u][0], dq);
         } else {
-          out[2 * q] = P::st(e);
-          out[2 * q + 1] = P::st(o);
+          V dt[H];
+#pragma unroll
+          for (int j = 0; j < H; j++) dt[j] = thr_v<P>(dv[u][j], th, l);
+          typename P::Acc ae = P::acc_init(sv[u][H - 1], tap_h(F, 2 * (H - 1)));
+          typename P::Acc ao = P::acc_init(sv[u][H - 1], tap_h(F, 2 * (H - 1) + 1));
+          ae = P::acc_add(ae, dt[H - 1], tap_g(F, 2 * (H - 1)));
+          ao = P::acc_add(ao, dt[H - 1], tap_g(F, 2 * (H - 1) + 1));
+#pragma unroll
+          for (int j = H - 2; j >= 0; j--) {
+            ae = P::acc_add(ae, sv[u][j], tap_h(F, 2 * j));
+            ao = P::acc_add(ao, sv[u][j], tap_h(F, 2 * j + 1));
+            ae = P::acc_add(ae, dt[j], tap_g(F, 2 * j));
+            ao = P::acc_add(ao, dt[j], tap_g(F, 2 * j + 1));
+          }
+          e = P::acc_fin(ae);
+          o = P::acc_fin(ao);
         }
-      } else {
-        dstv[2 * q] = e;
-        dstv[2 * q + 1] = o;
+        if (l == 0) {
+          if constexpr (std::is_same<D, typename P::V>::value) {
+            out[2 * q] = e;
+            out[2 * q + 1] = o;
+          } else {
+            out[2 * q] = P::st(e);
+            out[2 * q + 1] = P::st(o);
+          }
+        } else {
+          dstv[2 * q] = e;
+          dstv[2 * q + 1] = o;
+        }
       }
-    }
+    });
     __syncthreads();
     Nl <<= 1;
   }
@@ -233,26 +264,6 @@ __device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_
 
 // ----------------------------------------------------- MODWT (block) ----
 // Stored coefficients: det = [d_1 | ... | d_J] (J blocks of N), sJ (N).
-
-// Outputs per thread per sweep of the block-level MODWT loops: the taps of
-// U outputs are loaded before any is combined, so that U * L independent
-// loads are in flight per thread (the sequences live in global memory).
-// Full sweeps of U outputs carry no bounds checks; the remainder runs one
-// output at a time.  FP32 takes 4 outputs; the 8-byte value types (FP64,
-// double-float) are arithmetic-bound and keep one (measured: two outputs
-// per thread slowed the double-float batch by 30 %).
-template <class V>
-constexpr int mod_unroll() {
-  return sizeof(V) == 4 ? 4 : 1;
-}
-
-template <int U, class Fn>
-__device__ __forceinline__ void sweep_outputs(int64_t N, Fn fn) {
-  const int64_t B = blockDim.x, step = U * B, full = (N / step) * step;
-  int64_t i0 = threadIdx.x;
-  for (; i0 < full; i0 += step) fn(std::integral_constant<int, U>{}, i0);
-  for (; i0 < N; i0 += B) fn(std::integral_constant<int, 1>{}, i0);
-}
 
 template <int F, class P, class S>
 __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, int64_t N, int J,

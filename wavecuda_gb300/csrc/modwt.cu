@@ -487,3 +487,171 @@ extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, 
   if (inv_ms) *inv_ms = bi;
   return rc;
 }
+
+// ---------------------------------------------------------------------------
+// Packet-ordered MODWT (code 2; fHaarMODWT/bHaarMODWT, haar.cpp:305-398, and
+// fDaub4MODWTpo/bDaub4MODWTpo, daub4.cpp:392-484 of the reference; C6 and
+// LA8 by the same rules).  Its forward coefficients are the time-ordered
+// ones stored per packet: level l's packet sh holds the (s, d) pairs of time
+// positions rev(sh, l+1) + 2^(l+1) k, interleaved (convert_modwt_level,
+// wavutils.cpp:569-600).  Its inverse differs in arithmetic: every packet is
+// inverted one DWT level and each packet pair's two reconstructions are
+// averaged (writeavpackets, wavutils.cpp:304-330).  Here the inverse works on
+// the time-ordered copy: output u = st + 2^l i of level l-1 averages packet
+// residue st at packet position i with residue st + 2^l at position i - 1.
+
+namespace wc {
+namespace {
+
+template <class T>
+__global__ void modwt_layout_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
+                                    int log2n, int J, int to_po) {
+  const int64_t total = 2 * n * (int64_t)J;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += stride) {
+    const int l = (int)(idx / (2 * n));
+    const int64_t base = (int64_t)l * 2 * n, e = idx - base;
+    const int64_t skip = (int64_t)1 << l, lenos = n >> l;
+    const int64_t sh = e >> (log2n - l), w = e & (lenos - 1), k = w >> 1;
+    const int64_t st = (int64_t)(__brev((unsigned)sh) >> (31 - l));
+    const int64_t te = ((w & 1) ? n : 0) + st + 2 * skip * k;
+    if (to_po) out[base + e] = in[base + te];
+    else out[base + te] = in[base + e];
+  }
+}
+
+// One value of the one-level inverse DWT of the packet whose pairs are
+// (S, D)[r + 2 skip q], q < Pq, at packet position i (the arithmetic of
+// bHaar / bDaub4 / bC6 / bLA8: taps in descending j, s before d).
+template <int F, class P>
+__device__ __forceinline__ typename P::V po_packet_inv(const typename P::T* S,
+                                                       const typename P::T* D, int64_t r,
+                                                       int64_t skip, int64_t Pq, int64_t i) {
+  using V = typename P::V;
+  const int64_t q = i >> 1;
+  const bool odd = (i & 1) != 0;
+  if constexpr (F == 1) {
+    const V a = P::ld(S[r + 2 * skip * q]), b = P::ld(D[r + 2 * skip * q]);
+    return odd ? haar_dif<P>(a, b) : haar_sum<P>(a, b);
+  } else {
+    constexpr int HH = filter_len(F) / 2;
+    V sv[HH], dv[HH];
+#pragma unroll
+    for (int j = 0; j < HH; j++) {
+      const int64_t p = (q - j) & (Pq - 1);
+      sv[j] = P::ld(S[r + 2 * skip * p]);
+      dv[j] = P::ld(D[r + 2 * skip * p]);
+    }
+    typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
+    typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
+    ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
+    ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
+#pragma unroll
+    for (int j = HH - 2; j >= 0; j--) {
+      ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
+      ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
+      ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
+      ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
+    }
+    return odd ? P::acc_fin(ao) : P::acc_fin(ae);
+  }
+}
+
+template <int F, class P>
+__global__ void __launch_bounds__(kThreads)
+modwt_po_inv_level(const typename P::T* __restrict__ S, const typename P::T* __restrict__ D,
+                   typename P::T* __restrict__ out, int64_t n, int l) {
+  const int64_t skip = (int64_t)1 << l, lenos = n >> l, Pq = lenos >> 1;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
+    const int64_t st = u & (skip - 1), i = u >> l;
+    const typename P::V a = po_packet_inv<F, P>(S, D, st, skip, Pq, i);
+    const typename P::V b =
+        po_packet_inv<F, P>(S, D, st + skip, skip, Pq, (i + lenos - 1) & (lenos - 1));
+    out[u] = P::st(P::half(P::add(a, b)));
+  }
+}
+
+unsigned po_grid(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 16));
+}
+
+template <int F, class P>
+int run_po_inverse(const typename P::T* xmod, typename P::T* x, int64_t n, int J,
+                   cudaStream_t s) {
+  using T = typename P::T;
+  T* tmp[2] = {nullptr, nullptr};
+  if (J > 1) {
+    tmp[0] = static_cast<T*>(workspace(kSlotModwt0, sizeof(T) * (size_t)n));
+    tmp[1] = static_cast<T*>(workspace(kSlotModwt1, sizeof(T) * (size_t)n));
+    if (!tmp[0] || !tmp[1]) return workspace_error();
+  }
+  const T* S = xmod + (int64_t)2 * (J - 1) * n;
+  for (int l = J - 1; l >= 0; l--) {
+    T* out = (l == 0) ? x : tmp[l & 1];
+    {
+      LaunchTimer lt("modwt_po_inv_level", s);
+      modwt_po_inv_level<F, P><<<po_grid(n), kThreads, 0, s>>>(S, xmod + (int64_t)(2 * l + 1) * n,
+                                                              out, n, l);
+    }
+    WC_TRY(after_launch("modwt_po_inv_level"));
+    S = out;
+  }
+  return WC_OK;
+}
+
+template <class P>
+int dispatch_po_inverse(const void* xmod, void* x, int64_t n, int J, int F, cudaStream_t s) {
+  using T = typename P::T;
+  const T* xm = static_cast<const T*>(xmod);
+  T* xo = static_cast<T*>(x);
+  switch (F) {
+    case 1: return run_po_inverse<1, P>(xm, xo, n, J, s);
+    case 2: return run_po_inverse<2, P>(xm, xo, n, J, s);
+    case 3: return run_po_inverse<3, P>(xm, xo, n, J, s);
+    case 4: return run_po_inverse<4, P>(xm, xo, n, J, s);
+  }
+  return fail(WC_ERR_ARG, "unknown filter %d", F);
+}
+
+}  // namespace
+
+int modwt_layout(const void* in, void* out, int64_t n, int J, int to_po, int prec,
+                 cudaStream_t s) {
+  int log2n = 0;
+  while (((int64_t)1 << log2n) < n) log2n++;
+  const int64_t total = 2 * n * (int64_t)J;
+  LaunchTimer lt("modwt_layout", s);
+  if (prec == WC_F32)
+    modwt_layout_kernel<float><<<po_grid(total), kThreads, 0, s>>>(
+        static_cast<const float*>(in), static_cast<float*>(out), n, log2n, J, to_po);
+  else
+    modwt_layout_kernel<double><<<po_grid(total), kThreads, 0, s>>>(
+        static_cast<const double*>(in), static_cast<double*>(out), n, log2n, J, to_po);
+  return after_launch("modwt_layout_kernel");
+}
+
+int modwt_po_inverse_to(void* x, const void* xmod, int64_t n, int J, int F, int prec,
+                        cudaStream_t s) {
+  switch (prec) {
+    case WC_F64_EXACT: return dispatch_po_inverse<PExact>(xmod, x, n, J, F, s);
+    case WC_F64_FAST: return dispatch_po_inverse<PDD>(xmod, x, n, J, F, s);
+    case WC_F32: return dispatch_po_inverse<PF32>(xmod, x, n, J, F, s);
+  }
+  return fail(WC_ERR_ARG, "unknown precision %d", prec);
+}
+
+int modwt_po(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec, cudaStream_t s) {
+  const size_t es = (prec == WC_F32) ? 4 : 8;
+  void* to = workspace(kSlotPacket, es * 2 * (size_t)n * (size_t)J);
+  if (!to) return workspace_error();
+  if (sense == 1) {
+    WC_TRY(modwt(x, to, n, 1, J, F, prec, s));
+    return modwt_layout(to, xmod, n, J, 1, prec, s);
+  }
+  WC_TRY(modwt_layout(xmod, to, n, J, 0, prec, s));
+  return modwt_po_inverse_to(x, to, n, J, F, prec, s);
+}
+
+}  // namespace wc

@@ -119,6 +119,7 @@ struct Ctx {
   int64_t n, lenh;
   int J, ttype, F, hardness, minl, maxl, prec, copy_scaling;
   cudaStream_t s;
+  bool po;  // packet-ordered MODWT: time-ordered store, packet-ordered inverse
 };
 
 template <class T>
@@ -127,6 +128,7 @@ int transform_full(const Ctx<T>& c, void* x, void* coef, int64_t len, int J, int
     return sense == 1 ? dwt(x, coef, len, 1, J, c.F, c.prec, c.s)
                       : dwt(coef, x, len, 0, J, c.F, c.prec, c.s);
   }
+  if (sense == 0 && c.po) return modwt_po_inverse_to(x, coef, len, J, c.F, c.prec, c.s);
   return modwt(x, coef, len, sense, J, c.F, c.prec, c.s);
 }
 
@@ -146,7 +148,8 @@ int half_step(const Ctx<T>& c, const T* wcoef, HalfVec<T>& y, double t) {
     WC_TRY(dwt(y.buf[y.cur], y.buf[1 - y.cur], c.lenh, 0, lv1, c.F, c.prec, c.s));
     y.cur = 1 - y.cur;
   } else {
-    WC_TRY(modwt(y.buf[0], y.mod, c.lenh, 0, lv1, c.F, c.prec, c.s));
+    if (c.po) WC_TRY(modwt_po_inverse_to(y.buf[0], y.mod, c.lenh, lv1, c.F, c.prec, c.s));
+    else WC_TRY(modwt(y.buf[0], y.mod, c.lenh, 0, lv1, c.F, c.prec, c.s));
   }
   y.transformed = 0;
   return WC_OK;
@@ -183,7 +186,12 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
                 int hardness, int minl, int maxl, double tol, int prec, cudaStream_t s,
                 wc_smooth_info* info) {
   const int L = filter_len(F);
-  Ctx<T> c{n, n / 2, J, ttype, F, hardness, minl, maxl, prec, 0, s};
+  // Packet order (code 2) keeps its coefficients in time order here: the
+  // thresholds, the universal threshold's MAD and the kept counts see the
+  // same values; only the inverse differs (modwt_po_inverse_to).
+  const bool po = (ttype == 2);
+  if (po) ttype = 1;
+  Ctx<T> c{n, n / 2, J, ttype, F, hardness, minl, maxl, prec, 0, s, po};
   const int64_t lenh = n / 2;
   const int64_t wlen = (ttype == 0) ? n : 2 * n * (int64_t)J;
   const int64_t hlen = (ttype == 0) ? lenh : 2 * lenh * (int64_t)std::max(J - 1, 1);

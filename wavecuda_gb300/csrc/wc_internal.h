@@ -67,6 +67,7 @@ enum Slot {
   kSlotBatch,        // batched smoothing (descriptors, results, CTA scratch)
   kSlotAdjoint,      // loss / gradient evaluation (coefficients, cotangents)
   kSlotTune,         // batched threshold tuning (coefficients, state)
+  kSlotPacket,       // packet-ordered MODWT: time-ordered copy of the coefficients
   kNumSlots
 };
 
@@ -101,6 +102,19 @@ int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
 // short for chunking or the precision is FP32.  Enqueues on s; the caller
 // synchronises.
 int dwt_host_inplace(double* x, int64_t n, int sense, int J, int F, int prec, cudaStream_t s);
+
+// Packet-ordered MODWT (code 2, haar.cpp:305-398, daub4.cpp:392-484).
+// FWD: x -> xmod in packet order.  BWD: xmod (packet order, not modified) ->
+// x, averaging packet-pair reconstructions as the reference does.
+int modwt_po(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec, cudaStream_t s);
+// Per-level permutation of a 2*n*J MODWT array between time order and
+// packet order (to_po 1: time -> packet), out of place.
+int modwt_layout(const void* in, void* out, int64_t n, int J, int to_po, int prec,
+                 cudaStream_t s);
+// Inverse of a time-ordered coefficient array with the packet-ordered
+// transform's arithmetic (xmod not modified).
+int modwt_po_inverse_to(void* x, const void* xmod, int64_t n, int J, int F, int prec,
+                        cudaStream_t s);
 
 // Time-ordered MODWT.  FWD: x -> xmod.  BWD: xmod -> x (xmod not modified).
 int modwt(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec,
