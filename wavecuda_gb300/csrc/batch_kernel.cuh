@@ -435,8 +435,15 @@ __device__ void bselect(const Src<T>& src, long long ka, long long kb, SelShared
     for_each_src(src, [&](double v) {
       const uint64_t k = key_of(v);
       const int d = (int)((k >> shift) & 255);
-      if ((k & m0) == p0) atomicAdd(&sh.h[0][d], 1u);
-      if ((k & m1) == p1) atomicAdd(&sh.h[1][d], 1u);
+      // Lanes of a warp that hit the same bin add once (the values of a
+      // selection cluster in few bins, so per-lane atomics serialise).
+      const unsigned act = __activemask();
+      const unsigned b0 = ((k & m0) == p0) ? (unsigned)d : 256u;
+      const unsigned b1 = ((k & m1) == p1) ? (unsigned)d : 256u;
+      const unsigned g0 = __match_any_sync(act, b0), g1 = __match_any_sync(act, b1);
+      const int lane = threadIdx.x & 31;
+      if (b0 < 256u && lane == __ffs(g0) - 1) atomicAdd(&sh.h[0][b0], (unsigned)__popc(g0));
+      if (b1 < 256u && lane == __ffs(g1) - 1) atomicAdd(&sh.h[1][b1], (unsigned)__popc(g1));
     });
     __syncthreads();
     if (threadIdx.x < 2) {
@@ -471,7 +478,13 @@ __device__ void bmedian_mad(const Src<T>& src, double* dev_buf, SelShared& sh, d
   if (threadIdx.x == 0) pos = 0;
   __syncthreads();
   for_each_src(src, [&](double v) {
-    const unsigned long long k = atomicAdd(&pos, 1ull);
+    // one atomic per warp; lanes take consecutive slots
+    const unsigned act = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(&pos, (unsigned long long)__popc(act));
+    base = __shfl_sync(act, base, leader);
+    const unsigned long long k = base + __popc(act & ((1u << lane) - 1u));
     dev_buf[k] = fabs(__dsub_rn(v, m));
   });
   __syncthreads();

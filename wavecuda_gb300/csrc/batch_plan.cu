@@ -25,6 +25,7 @@ struct wc_batch_plan_s {
   int* d_order = nullptr;
   int* d_counter = nullptr;
   char* d_scratch = nullptr;
+  bool own_scratch = true;  // false: the scratch is the library workspace
   size_t scratch_bytes = 0;
   // graph cache
   cudaGraphExec_t exec = nullptr;
@@ -49,7 +50,7 @@ void free_plan(wc_batch_plan_s* p) {
   cudaFree(p->d_res);
   cudaFree(p->d_order);
   cudaFree(p->d_counter);
-  cudaFree(p->d_scratch);
+  if (p->own_scratch) cudaFree(p->d_scratch);
   delete p;
 }
 
@@ -72,7 +73,26 @@ using namespace wc;
 
 extern "C" {
 
+namespace wc {
+namespace {
+int plan_create(const wc_signal* sigs, int nsig, int precision, bool workspace_scratch,
+                wc_batch_plan* out);
+}  // namespace
+}  // namespace wc
+
 int wc_batch_plan_create(const wc_signal* sigs, int nsig, int precision, wc_batch_plan* out) {
+  return wc::plan_create(sigs, nsig, precision, false, out);
+}
+
+}  // extern "C"
+
+namespace wc {
+namespace {
+
+// workspace_scratch: the CTA scratch comes from the library's per-device
+// workspace (kept between calls), for the synchronous host-buffer call.
+int plan_create(const wc_signal* sigs, int nsig, int precision, bool workspace_scratch,
+                wc_batch_plan* out) {
   clear_error();
   if (!sigs || nsig <= 0 || !out) return fail(WC_ERR_ARG, "bad batch arguments");
   if (precision < 0 || precision > 2) return fail(WC_ERR_ARG, "unknown precision %d", precision);
@@ -137,10 +157,18 @@ int wc_batch_plan_create(const wc_signal* sigs, int nsig, int precision, wc_batc
       (e = cudaMalloc(&p->d_res, sizeof(BatchResult) * nsig)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_order, sizeof(int) * nsig)) != cudaSuccess ||
       (e = cudaMalloc(&p->d_counter, sizeof(int))) != cudaSuccess ||
-      (e = cudaMalloc(&p->d_scratch, p->scratch_bytes)) != cudaSuccess) {
+      (!workspace_scratch && (e = cudaMalloc(&p->d_scratch, p->scratch_bytes)) != cudaSuccess)) {
     cudaGetLastError();
     free_plan(p);
     return fail(WC_ERR_NOMEM, "batch plan allocation failed: %s", cudaGetErrorString(e));
+  }
+  if (workspace_scratch) {
+    p->own_scratch = false;
+    p->d_scratch = static_cast<char*>(workspace(kSlotBatchScratch, p->scratch_bytes));
+    if (!p->d_scratch) {
+      free_plan(p);
+      return workspace_error();
+    }
   }
   cudaMemcpy(p->d_desc, desc.data(), sizeof(BatchDesc) * nsig, cudaMemcpyHostToDevice);
   cudaMemcpy(p->d_order, order.data(), sizeof(int) * nsig, cudaMemcpyHostToDevice);
@@ -148,6 +176,11 @@ int wc_batch_plan_create(const wc_signal* sigs, int nsig, int precision, wc_batc
   *out = p;
   return WC_OK;
 }
+
+}  // namespace
+}  // namespace wc
+
+extern "C" {
 
 int wc_batch_plan_destroy(wc_batch_plan plan) {
   free_plan(plan);
@@ -271,7 +304,7 @@ int wc_smooth_batch(double* data, int64_t total, const wc_signal* sigs, int nsig
     if (sigs[i].offset + sigs[i].len > total)
       return fail(WC_ERR_ARG, "signal %d extends past the data (%lld elements)", i, (long long)total);
   wc_batch_plan plan = nullptr;
-  WC_TRY(wc_batch_plan_create(sigs, nsig, precision, &plan));
+  WC_TRY(wc::plan_create(sigs, nsig, precision, true, &plan));
   cudaStream_t s = lib_stream();
   double* d = static_cast<double*>(workspace(kSlotBatch, sizeof(double) * (size_t)total));
   int rc = d ? WC_OK : workspace_error();

@@ -891,6 +891,14 @@ int dwt(const void* in, void* out, int64_t n, int sense, int J, int F, int prec,
 // host page tables, such as Grace); callers check that.
 namespace {
 
+template <class T>
+__global__ void gather_stride_kernel(const T* __restrict__ src, T* __restrict__ dst, int64_t count,
+                                     int shift) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+    dst[i] = src[i << shift];
+}
+
 struct HostStreamState {
   cudaStream_t up = nullptr;
   cudaEvent_t ev[kHostChunksMax] = {};
@@ -991,9 +999,26 @@ int run_dwt_host(typename P::T* x, int64_t n, int sense, int J, cudaStream_t s) 
   }
   // Inverse: coarse passes straight from the host array, then the first
   // pass chunk by chunk (chunk 0 last: its left halo wraps to the end).
+  // The coarse passes read only the slots q 2^G0 of the host array: one
+  // gather kernel with many reads in flight brings them to the device first.
   auto ikern = dwt_inv_pass<F, P>;
-  const T* coarse = x;
-  int64_t cstride = plan[np - 1].S << plan[np - 1].G;
+  const T* cin = x;
+  int sh = 0;
+  if (np > 1) {
+    const int64_t cnt = p0.N >> p0.G;
+    T* C = static_cast<T*>(workspace(kSlotHostCoarse, sizeof(T) * (size_t)cnt));
+    if (!C) return workspace_error();
+    {
+      LaunchTimer lt("gather_stride", s);
+      const int64_t blocks = std::min<int64_t>((cnt + kThreads - 1) / kThreads, 152 * 32);
+      gather_stride_kernel<T><<<(unsigned)blocks, kThreads, 0, s>>>(x, C, cnt, p0.G);
+    }
+    WC_TRY(after_launch("gather_stride_kernel"));
+    cin = C;
+    sh = p0.G;
+  }
+  const T* coarse = cin;
+  int64_t cstride = (plan[np - 1].S << plan[np - 1].G) >> sh;
   for (int p = np - 1; p >= 1; p--) {
     const PassPlan& pp = plan[p];
     T* dst = scratch[p & 1];
@@ -1002,8 +1027,8 @@ int run_dwt_host(typename P::T* x, int64_t n, int sense, int J, cudaStream_t s) 
     WC_CUDA(cudaFuncSetAttribute(ikern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     {
       LaunchTimer lt("dwt_inv_pass", s);
-      ikern<<<(unsigned)(pp.N / pp.Tt), kThreads, sm, s>>>(coarse, cstride, x, pp.S, pp.N, pp.G,
-                                                          pp.Tt, dst, 1, geo, 0, status, 0);
+      ikern<<<(unsigned)(pp.N / pp.Tt), kThreads, sm, s>>>(coarse, cstride, cin, pp.S >> sh, pp.N,
+                                                          pp.G, pp.Tt, dst, 1, geo, 0, status, 0);
     }
     WC_TRY(after_launch("dwt_inv_pass"));
     coarse = dst;

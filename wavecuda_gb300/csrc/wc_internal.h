@@ -68,6 +68,8 @@ enum Slot {
   kSlotAdjoint,      // loss / gradient evaluation (coefficients, cotangents)
   kSlotTune,         // batched threshold tuning (coefficients, state)
   kSlotPacket,       // packet-ordered MODWT: time-ordered copy of the coefficients
+  kSlotBatchScratch, // batched smoothing through the host-buffer call: CTA scratch
+  kSlotHostCoarse,   // host-streamed DWT: coarse slots gathered from the host array
   kNumSlots
 };
 
