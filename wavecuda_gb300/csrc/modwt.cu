@@ -28,6 +28,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
 
@@ -106,11 +107,18 @@ modwt_fwd_tiled(const typename P::T* __restrict__ X, typename P::T* __restrict__
   const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
   const int cs = __ffs(C) - 1;  // C is a power of two
   const int tot = (M + HR) * C;
-  // Unrolled so that each thread keeps several independent loads in flight.
-#pragma unroll 8
+  // Raw values arrive by per-thread asynchronous copies (all in flight at
+  // once), then each thread converts its own in place.
+  using T = typename P::T;
+  static_assert(sizeof(T) == sizeof(V), "in-place staging");
+  T* In_raw = reinterpret_cast<T*>(In);
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const int row = e >> cs, c = e & (C - 1);
-    In[e] = P::ld(X[(r0 + c) + ((m0 + row) & (nrows - 1)) * d0]);
+    cp_async_elem(In_raw + e, X + (r0 + c) + ((m0 + row) & (nrows - 1)) * d0);
+  }
+  cp_async_wait_all();
+  if constexpr (!std::is_same<T, V>::value) {
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) In[e] = P::ld(In_raw[e]);
   }
   __syncthreads();
   typename P::T* S0 = xmod + (int64_t)2 * l0 * n;
@@ -165,14 +173,27 @@ modwt_inv_tiled(const typename P::T* __restrict__ Stop, const typename P::T* __r
   const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
   const int cs = __ffs(C) - 1;
   const int tot = R * C;
-#pragma unroll 4
+  // Raw values arrive by per-thread asynchronous copies (every copy of the
+  // tile in flight at once), then each thread converts its own in place.
+  using T = typename P::T;
+  static_assert(sizeof(T) == sizeof(V), "in-place staging");
+  T* St_raw = reinterpret_cast<T*>(St);
+  T* Db_raw = reinterpret_cast<T*>(Db);
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const int row = e >> cs, c = e & (C - 1);
     const int64_t g = (r0 + c) + ((m0 - HR + row) & (nrows - 1)) * d0;
-    St[e] = P::ld(Stop[g]);
+    cp_async_elem(St_raw + e, Stop + g);
 #pragma unroll
     for (int t = 0; t < NI; t++)
-      Db[t * tot + e] = P::ld(xmod[(int64_t)(2 * (l0 + t) + 1) * n + g]);
+      cp_async_elem(Db_raw + t * tot + e, xmod + (int64_t)(2 * (l0 + t) + 1) * n + g);
+  }
+  cp_async_wait_all();
+  if constexpr (!std::is_same<T, V>::value) {
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      St[e] = P::ld(St_raw[e]);
+#pragma unroll
+      for (int t = 0; t < NI; t++) Db[t * tot + e] = P::ld(Db_raw[t * tot + e]);
+    }
   }
   __syncthreads();
   const V* cur = St;

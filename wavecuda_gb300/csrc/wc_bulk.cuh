@@ -91,4 +91,24 @@ __device__ __forceinline__ bool aligned16(const void* p) {
   return (reinterpret_cast<uintptr_t>(p) & 15) == 0;
 }
 
+// Per-thread asynchronous copy of one 4- or 8-byte element from global to
+// shared memory (cp.async, sm_80 and later): the load needs no register, so a
+// thread can keep all its copies in flight at once.  cp_async_wait_all()
+// waits for the calling thread's copies (a hardware wait on plain loads,
+// which always complete).
+template <class T>
+__device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(smem_dst)), "l"(gsrc)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem_dst)), "l"(gsrc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 }  // namespace wc
