@@ -679,7 +679,9 @@ std::vector<PassPlan> plan_passes_cfg(int64_t n, int J, int F, const TileCfg& c)
   int l = 0;
   while (l < J) {
     const bool first = plan.empty();
-    const int64_t Tt = std::min(N, first ? (int64_t)c.tile : TT);
+    int64_t Tt = std::min(N, first ? (int64_t)c.tile : TT);
+    // Later passes are short: smaller tiles keep every SM busy.
+    while (!first && Tt > 1024 && N / Tt < 2 * 152) Tt >>= 1;
     int G = std::min(J - l, (Tt == N) ? 30 : (first ? c.g0 : gmax));
     auto fits = [&](int g) {
       if (first && c.pipe && Tt < N)
