@@ -269,15 +269,15 @@ def ours(args):
         if not args.no_sweep:
             combos |= {(f, p) for f in (1, 2, 3, 4) for p in (0, 1, 2)}
         for f, p in sorted(combos):
-            (tile, g0, th, pipe), tms = wc.tune_dwt(f, p, 24)
+            (tile, g0, th, pipe), tms = wc.tune_dwt(f, p, args.log2n)
             tiling[f"{FILTERS[f]}/{PREC[p]}"] = {"tile": tile, "g0": g0, "threads": th,
-                                                  "pipelined": pipe, "ms_2e24": round(tms, 4)}
+                                                  "pipelined": pipe, "fwd_inv_ms": round(tms, 4)}
         if not args.no_sweep:
             for f, p in sorted({(f, p) for f in (1, 2, 3, 4) for p in (0, 1, 2)}):
-                mt, fms, ims = wc.tune_modwt(f, p, 24, 12)
+                mt, fms, ims = wc.tune_modwt(f, p, args.log2n, 12)
                 tiling[f"MODWT {FILTERS[f]}/{PREC[p]}"] = {
                     "fwd_target": mt[0], "fwd_smem_kb": mt[1], "inv_target": mt[2],
-                    "inv_smem_kb": mt[3], "fwd_ms_2e24": round(fms, 4), "inv_ms_2e24": round(ims, 4)}
+                    "inv_smem_kb": mt[3], "fwd_ms": round(fms, 4), "inv_ms": round(ims, 4)}
 
     clocks = ClockSampler()
     clocks.start()

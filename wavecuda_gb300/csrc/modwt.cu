@@ -89,6 +89,27 @@ __device__ __forceinline__ typename P::V inv_taps(const typename P::V* S, const 
   }
 }
 
+// Two adjacent inverse outputs (S, D and S + 1, D + 1) in double-float with
+// packed pairs: per lane the operations of inv_taps, so the same bits.
+template <int F>
+__device__ __forceinline__ void inv_taps2_dd(const dd* S, const dd* D, int stride, dd& r0, dd& r1) {
+  constexpr int L = filter_len(F);
+  dd_acc2 A;
+#pragma unroll
+  for (int t = 0; t < L; t++) {
+    const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
+    const tap2 h = make_tap2(tap_h(F, k), tap_h(F, k)), g = make_tap2(tap_g(F, k), tap_g(F, k));
+    const dd* s = S - k * stride;
+    const dd* d = D - k * stride;
+    if (t == 0) A = acc2_init_xy(s[0], s[1], h);
+    else A = acc2_add_xy(A, s[0], s[1], h);
+    A = acc2_add_xy(A, d[0], d[1], g);
+  }
+  acc2_fin(A, r0, r1);
+  r0 = PDD::half(r0);
+  r1 = PDD::half(r1);
+}
+
 // Forward levels l0 .. l0+NF-1.  Tile: columns r0 .. r0+C-1, rows m0 ..
 // m0+M-1 of the row view with unit d0 = 2^l0 (nrows = n / d0 rows).
 template <int F, class P, int NF>
@@ -203,14 +224,28 @@ modwt_inv_tiled(const typename P::T* __restrict__ Stop, const typename P::T* __r
     const int a_lo = HR - (L - 1) * ((1 << t) - 1);
     V* dst = ((NI - 1 - t) & 1) ? B : A;
     const V* Dt = Db + t * tot;
-    for (int e = a_lo * C + threadIdx.x; e < tot; e += blockDim.x) {
-      const V v = inv_taps<F, P>(cur + e, Dt + e, rd * C);
+    auto put = [&](int e, V v) {
       if (t == 0) {
         const int row = e >> cs, c = e & (C - 1);
         out[(r0 + c) + (m0 - HR + row) * d0] = P::st(v);
       } else {
         dst[e] = v;
       }
+    };
+    if constexpr (std::is_same<P, PDD>::value && F != 1) {
+      // outputs in adjacent pairs, one packed dot product per pair
+      const int e0 = a_lo * C;
+      int e = e0 + 2 * (int)threadIdx.x;
+      for (; e + 1 < tot; e += 2 * blockDim.x) {
+        V v0, v1;
+        inv_taps2_dd<F>(cur + e, Dt + e, rd * C, v0, v1);
+        put(e, v0);
+        put(e + 1, v1);
+      }
+      if (((tot - e0) & 1) && threadIdx.x == 0) put(tot - 1, inv_taps<F, P>(cur + tot - 1, Dt + tot - 1, rd * C));
+    } else {
+      for (int e = a_lo * C + threadIdx.x; e < tot; e += blockDim.x)
+        put(e, inv_taps<F, P>(cur + e, Dt + e, rd * C));
     }
     if (t > 0) {
       __syncthreads();

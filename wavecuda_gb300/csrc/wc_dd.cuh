@@ -250,4 +250,28 @@ __device__ __forceinline__ void acc2_fin(dd_acc2 A, dd& r0, dd& r1) {
   r1 = {h1, l1};
 }
 
+// Two dot products with the same taps on different inputs (lane 0: input
+// a0, lane 1: input a1), e.g. two adjacent outputs of a filter.  The tap is
+// broadcast to both lanes.
+__device__ __forceinline__ dd_acc2 acc2_init_xy(dd a0, dd a1, const tap2& c) {
+  const f32x2 ah = x2_pack(a0.hi, a1.hi), al = x2_pack(a0.lo, a1.lo);
+  const f32x2 p = x2_mul(ah, c.ch);
+  f32x2 ne = x2_fma(ah, c.nch, p);
+  ne = x2_fma(ah, c.ncl, ne);
+  ne = x2_fma(al, c.nch, ne);
+  return {p, ne};
+}
+
+__device__ __forceinline__ dd_acc2 acc2_add_xy(dd_acc2 A, dd a0, dd a1, const tap2& c) {
+  const f32x2 ah = x2_pack(a0.hi, a1.hi), al = x2_pack(a0.lo, a1.lo);
+  const f32x2 p = x2_mul(ah, c.ch);
+  f32x2 npe = x2_fma(ah, c.nch, p);
+  npe = x2_fma(ah, c.ncl, npe);
+  npe = x2_fma(al, c.nch, npe);
+  const f32x2 s = x2_add(A.s, p);
+  const f32x2 bb = x2_sub(s, A.s);
+  const f32x2 t = x2_add(x2_sub(A.s, x2_sub(s, bb)), x2_sub(p, bb));
+  return {s, x2_add(A.ne, x2_sub(npe, t))};
+}
+
 }  // namespace wc
