@@ -495,16 +495,24 @@ __global__ void __launch_bounds__(FT, 2) fit_batch_kernel(FitArgs a) {
 
 template <class P>
 int fit_launch_p(const FitArgs& a, int grid, cudaStream_t s) {
-  fit_batch_kernel<P><<<grid, FT, 0, s>>>(a);
+  constexpr size_t smem = mod_tile_smem<typename P::V>();
+  WC_CUDA(cudaFuncSetAttribute(fit_batch_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  fit_batch_kernel<P><<<grid, FT, smem, s>>>(a);
   return after_launch("fit_batch_kernel");
 }
 
 template <class P>
 int fit_blocks_per_sm_p() {
+  constexpr size_t smem = mod_tile_smem<typename P::V>();
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fit_batch_kernel<P>, FT, 0) !=
-      cudaSuccess)
+  if (cudaFuncSetAttribute(fit_batch_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fit_batch_kernel<P>, FT, smem) !=
+          cudaSuccess) {
+    cudaGetLastError();
     return 1;
+  }
   return per < 1 ? 1 : per;
 }
 

@@ -111,4 +111,14 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// Groups of per-thread asynchronous copies: commit closes the copies issued
+// since the last commit; wait_prior_1 waits until at most the newest group
+// is still in flight (double buffering).
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_prior_1() {
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+}
+
 }  // namespace wc
