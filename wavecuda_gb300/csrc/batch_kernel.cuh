@@ -315,53 +315,82 @@ __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, in
   }
 }
 
-// Shared-memory tiles of the block-level MODWT inverse (8-byte value types):
-// two arrays of kModTile values.  Kernels that run it are launched with
-// mod_tile_smem<V>() bytes of dynamic shared memory.
-constexpr int kModTile = 4096;
+// Shared-memory tiles of the block-level MODWT inverse: two stages of two
+// arrays (scaling values, details) of mod_tile<V>() values each.  Kernels
+// that run it are launched with mod_tile_smem<V>() bytes of dynamic shared
+// memory (16 KB per array either way, 64 KB per CTA).
+template <class V>
+constexpr int mod_tile() {
+  return sizeof(V) == 8 ? 2048 : 4096;
+}
 template <class V>
 constexpr size_t mod_tile_smem() {
-  return sizeof(V) == 8 ? 2 * (size_t)kModTile * sizeof(V) : 4 * (size_t)kModTile * sizeof(V);
+  return 4 * (size_t)mod_tile<V>() * sizeof(V);
 }
 
 // Inverse MODWT by tiles of the row view: level l splits the sequence into
 // d0 = 2^l interleaved columns whose taps are the rows above; a tile of C
-// adjacent columns (C = min(d0, 32)) by M rows plus the L-1 halo rows is
-// loaded once into shared memory (scaling values and thresholded details),
-// so every tap is a shared-memory read instead of a global one.  Each output
+// adjacent columns (C = min(d0, 32)) by M rows plus the L-1 halo rows sits
+// in shared memory, so every tap is a shared-memory read.  Each output
 // keeps the reference's term order (even taps then odd taps, s before d).
+// Tiled inverse with double buffering: the next tile's raw values arrive by
+// per-thread asynchronous copies while the current tile is computed, so the
+// load latency hides behind arithmetic even with one CTA per SM.  Each
+// thread converts (double-float) and thresholds the details it copied,
+// once, before the tile's barrier.
 template <int F, class P, class D, class TH>
-__device__ void bmodwt_inv_tiled(const typename P::T* det, const typename P::T* sJ, D* out,
-                                 int64_t N, int J, const TH& th, typename P::V* tA,
-                                 typename P::V* tB) {
+__device__ void bmodwt_inv_tiled2(const typename P::T* det, const typename P::T* sJ, D* out,
+                                  int64_t N, int J, const TH& th, typename P::V* tA,
+                                  typename P::V* tB) {
   using V = typename P::V;
   using T = typename P::T;
+  static_assert(sizeof(V) == sizeof(T), "in-place staging");
   constexpr int L = filter_len(F);
   constexpr int HR = L - 1;
+  constexpr int KT = mod_tile<V>();
   extern __shared__ __align__(16) unsigned char mod_smem[];
-  V* Ss = reinterpret_cast<V*>(mod_smem);
-  V* Ds = Ss + kModTile;
+  V* buf = reinterpret_cast<V*>(mod_smem);  // [stage][S | D][KT]
   for (int l = J - 1; l >= 0; l--) {
-    const V* src = ((J - 1 - l) & 1) ? tA : tB;  // s_{l+1} when l < J-1
+    const bool top = (l == J - 1);
+    const V* src = ((J - 1 - l) & 1) ? tA : tB;
     V* dst = ((J - 1 - l) & 1) ? tB : tA;
     const T* dl = det + (int64_t)l * N;
     const int64_t d0 = (int64_t)1 << l, rows = N >> l;
     const int C = (int)(d0 < 32 ? d0 : 32);
     const int cs = __ffs(C) - 1;
     int64_t M = rows;
-    while (M > 1 && (M + HR) * C > kModTile) M >>= 1;
+    while (M > 1 && (M + HR) * C > KT) M >>= 1;
     const int64_t nb = d0 / C, ntiles = nb * (rows / M);
     const int tot = (int)((M + HR) * C);
-    for (int64_t tile = 0; tile < ntiles; tile++) {
+    auto issue = [&](int64_t tile, int stage) {
+      V* Ss = buf + stage * 2 * KT;
+      V* Ds = Ss + KT;
       const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
-#pragma unroll 4
       for (int e = threadIdx.x; e < tot; e += blockDim.x) {
         const int row = e >> cs, c = e & (C - 1);
         const int64_t g = (r0 + c) + ((m0 - HR + row) & (rows - 1)) * d0;
-        Ss[e] = (l == J - 1) ? P::ld(sJ[g]) : src[g];
-        Ds[e] = thr_v<P>(P::ld(dl[g]), th, l);
+        if (top) cp_async_elem(reinterpret_cast<T*>(Ss) + e, sJ + g);
+        else cp_async_elem(Ss + e, src + g);
+        cp_async_elem(reinterpret_cast<T*>(Ds) + e, dl + g);
+      }
+      cp_async_commit();
+    };
+    issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+      const int stage = (int)(tile & 1);
+      if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
+      else cp_async_commit();  // empty group keeps the wait count uniform
+      cp_async_wait_prior_1();
+      V* Ss = buf + stage * 2 * KT;
+      V* Ds = Ss + KT;
+      for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+        if constexpr (!std::is_same<V, T>::value) {
+          if (top) Ss[e] = P::ld(reinterpret_cast<const T*>(Ss)[e]);
+        }
+        Ds[e] = thr_v<P>(P::ld(reinterpret_cast<const T*>(Ds)[e]), th, l);
       }
       __syncthreads();
+      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
       for (int e = HR * C + threadIdx.x; e < tot; e += blockDim.x) {
         const int row = e >> cs, c = e & (C - 1);
         V r;
@@ -389,101 +418,15 @@ __device__ void bmodwt_inv_tiled(const typename P::T* det, const typename P::T* 
           dst[i] = r;
         }
       }
-      __syncthreads();
-    }
-  }
-}
-
-// FP32 form of the tiled inverse with double buffering: the next tile's
-// values arrive by per-thread asynchronous copies while the current tile is
-// computed, so the load latency hides behind arithmetic even with one CTA
-// per SM.  Details are thresholded as they are read.
-template <int F, class P, class D, class TH>
-__device__ void bmodwt_inv_tiled2(const typename P::T* det, const typename P::T* sJ, D* out,
-                                  int64_t N, int J, const TH& th, typename P::V* tA,
-                                  typename P::V* tB) {
-  using V = typename P::V;
-  using T = typename P::T;
-  static_assert(std::is_same<V, T>::value, "raw copies need V == T");
-  constexpr int L = filter_len(F);
-  constexpr int HR = L - 1;
-  extern __shared__ __align__(16) unsigned char mod_smem[];
-  V* buf = reinterpret_cast<V*>(mod_smem);  // [stage][S | D][kModTile]
-  for (int l = J - 1; l >= 0; l--) {
-    const V* src = (l == J - 1) ? sJ : (((J - 1 - l) & 1) ? tA : tB);
-    V* dst = ((J - 1 - l) & 1) ? tB : tA;
-    const T* dl = det + (int64_t)l * N;
-    const int64_t d0 = (int64_t)1 << l, rows = N >> l;
-    const int C = (int)(d0 < 32 ? d0 : 32);
-    const int cs = __ffs(C) - 1;
-    int64_t M = rows;
-    while (M > 1 && (M + HR) * C > kModTile) M >>= 1;
-    const int64_t nb = d0 / C, ntiles = nb * (rows / M);
-    const int tot = (int)((M + HR) * C);
-    auto issue = [&](int64_t tile, int stage) {
-      V* Ss = buf + stage * 2 * kModTile;
-      V* Ds = Ss + kModTile;
-      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
-      for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-        const int row = e >> cs, c = e & (C - 1);
-        const int64_t g = (r0 + c) + ((m0 - HR + row) & (rows - 1)) * d0;
-        cp_async_elem(Ss + e, src + g);
-        cp_async_elem(Ds + e, dl + g);
-      }
-      cp_async_commit();
-    };
-    issue(0, 0);
-    for (int64_t tile = 0; tile < ntiles; tile++) {
-      const int stage = (int)(tile & 1);
-      if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
-      else cp_async_commit();  // empty group keeps the wait count uniform
-      cp_async_wait_prior_1();
-      __syncthreads();
-      const V* Ss = buf + stage * 2 * kModTile;
-      const V* Ds = Ss + kModTile;
-      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
-      for (int e = HR * C + threadIdx.x; e < tot; e += blockDim.x) {
-        const int row = e >> cs, c = e & (C - 1);
-        V r;
-        if constexpr (F == 1) {
-          V acc = P::add(Ss[e], thr_v<P>(Ds[e], th, l));
-          acc = P::add(acc, Ss[e - C]);
-          acc = P::sub(acc, thr_v<P>(Ds[e - C], th, l));
-          r = P::mul(acc, kHInvR2);
-        } else {
-          typename P::Acc acc;
-#pragma unroll
-          for (int t = 0; t < L; t++) {
-            const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
-            if (t == 0) acc = P::acc_init(Ss[e - k * C], tap_h(F, k));
-            else acc = P::acc_add(acc, Ss[e - k * C], tap_h(F, k));
-            acc = P::acc_add(acc, thr_v<P>(Ds[e - k * C], th, l), tap_g(F, k));
-          }
-          r = P::half(P::acc_fin(acc));
-        }
-        const int64_t i = (r0 + c) + (m0 - HR + row) * d0;
-        if (l == 0) {
-          if constexpr (std::is_same<D, V>::value) out[i] = r;
-          else out[i] = P::st(r);
-        } else {
-          dst[i] = r;
-        }
-      }
       __syncthreads();  // this stage is refilled two tiles later
     }
   }
 }
 
-// 8-byte value types (FP64 and double-float, arithmetic-heavy) read their
-// taps from shared-memory tiles; FP32 from global memory (measured: tiles
-// cost the FP32 batch 13 % and helped the double-float tuner 17 %).
 template <int F, class P, class D, class TH>
 __device__ void bmodwt_inv(const typename P::T* det, const typename P::T* sJ, D* out, int64_t N,
                            int J, const TH& th, typename P::V* tA, typename P::V* tB) {
-  if constexpr (sizeof(typename P::V) == 8)
-    bmodwt_inv_tiled<F, P, D, TH>(det, sJ, out, N, J, th, tA, tB);
-  else
-    bmodwt_inv_tiled2<F, P, D, TH>(det, sJ, out, N, J, th, tA, tB);
+  bmodwt_inv_tiled2<F, P, D, TH>(det, sJ, out, N, J, th, tA, tB);
 }
 
 // ------------------------------------------------- radix select (block) --
