@@ -266,55 +266,6 @@ __device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_
 // ----------------------------------------------------- MODWT (block) ----
 // Stored coefficients: det = [d_1 | ... | d_J] (J blocks of N), sJ (N).
 
-template <int F, class P, class S>
-__device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, int64_t N, int J,
-                           typename P::V* tA, typename P::V* tB) {
-  using V = typename P::V;
-  constexpr int L = filter_len(F);
-  const int64_t B = blockDim.x;
-  for (int l = 0; l < J; l++) {
-    const V* src = (l & 1) ? tA : tB;  // level l values (l >= 1)
-    V* dst = (l & 1) ? tB : tA;
-    const int64_t skip = (int64_t)1 << l;
-    typename P::T* dd_out = det + (int64_t)l * N;
-    sweep_outputs<mod_unroll<V>()>(N, [&](auto uc, int64_t i0) {
-      constexpr int UU = decltype(uc)::value;
-      V v[UU][L];
-#pragma unroll
-      for (int u = 0; u < UU; u++) {
-#pragma unroll
-        for (int k = 0; k < L; k++) {
-          const int64_t j = (i0 + u * B + (int64_t)k * skip) & (N - 1);
-          v[u][k] = (l == 0) ? rd<P>(x, j) : src[j];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < UU; u++) {
-        const int64_t i = i0 + u * B;
-        V s, d;
-        if constexpr (F == 1) {
-          d = haar_dif<P>(v[u][0], v[u][1]);
-          s = haar_sum<P>(v[u][0], v[u][1]);
-        } else {
-          typename P::Acc ad = P::acc_init(v[u][0], tap_g(F, 0));
-          typename P::Acc as = P::acc_init(v[u][0], tap_h(F, 0));
-#pragma unroll
-          for (int k = 1; k < L; k++) {
-            ad = P::acc_add(ad, v[u][k], tap_g(F, k));
-            as = P::acc_add(as, v[u][k], tap_h(F, k));
-          }
-          d = P::acc_fin(ad);
-          s = P::acc_fin(as);
-        }
-        dd_out[i] = P::st(d);
-        if (l == J - 1) sJ[i] = P::st(s);
-        else dst[i] = s;
-      }
-    });
-    __syncthreads();
-  }
-}
-
 // Shared-memory tiles of the block-level MODWT inverse: two stages of two
 // arrays (scaling values, details) of mod_tile<V>() values each.  Kernels
 // that run it are launched with mod_tile_smem<V>() bytes of dynamic shared
@@ -326,6 +277,94 @@ constexpr int mod_tile() {
 template <class V>
 constexpr size_t mod_tile_smem() {
   return 4 * (size_t)mod_tile<V>() * sizeof(V);
+}
+
+// One forward level (taps 2^l apart) by double-buffered shared-memory tiles
+// of the row view (taps are the L-1 rows below an output): the tile's raw
+// inputs arrive by per-thread asynchronous copies while the previous tile is
+// computed; emit(i, s, d) receives every output's scaling and detail value.
+template <int F, class P, class S, class Emit>
+__device__ void bfwd_level_tiled(const S* src, int64_t N, int l, Emit&& emit) {
+  using V = typename P::V;
+  static_assert(sizeof(S) == sizeof(V), "in-place staging");
+  constexpr int L = filter_len(F);
+  constexpr int HR = L - 1;
+  constexpr int KT = mod_tile<V>();
+  extern __shared__ __align__(16) unsigned char mod_smem[];
+  V* buf = reinterpret_cast<V*>(mod_smem);  // [stage][KT]
+  const int64_t d0 = (int64_t)1 << l, rows = N >> l;
+  const int C = (int)(d0 < 32 ? d0 : 32);
+  const int cs = __ffs(C) - 1;
+  int64_t M = rows;
+  while (M > 1 && (M + HR) * C > KT) M >>= 1;
+  const int64_t nb = d0 / C, ntiles = nb * (rows / M);
+  const int tot = (int)((M + HR) * C);
+  auto issue = [&](int64_t tile, int stage) {
+    S* Vs = reinterpret_cast<S*>(buf + stage * KT);
+    const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int row = e >> cs, c = e & (C - 1);
+      cp_async_elem(Vs + e, src + (r0 + c) + ((m0 + row) & (rows - 1)) * d0);
+    }
+    cp_async_commit();
+  };
+  issue(0, 0);
+  for (int64_t tile = 0; tile < ntiles; tile++) {
+    const int stage = (int)(tile & 1);
+    if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
+    else cp_async_commit();  // empty group keeps the wait count uniform
+    cp_async_wait_prior_1();
+    V* Vs = buf + stage * KT;
+    if constexpr (!std::is_same<S, V>::value) {
+      for (int e = threadIdx.x; e < tot; e += blockDim.x)
+        Vs[e] = P::ld(reinterpret_cast<const S*>(Vs)[e]);
+    }
+    __syncthreads();
+    const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+    for (int e = threadIdx.x; e < (int)(M * C); e += blockDim.x) {
+      const int row = e >> cs, c = e & (C - 1);
+      V s, d;
+      if constexpr (F == 1) {
+        d = haar_dif<P>(Vs[e], Vs[e + C]);
+        s = haar_sum<P>(Vs[e], Vs[e + C]);
+      } else if constexpr (std::is_same<P, PDD>::value) {
+        // d in lane 0, s in lane 1: the operations below, packed
+        dd_acc2 A = acc2_init(Vs[e], make_tap2(tap_g(F, 0), tap_h(F, 0)));
+#pragma unroll
+        for (int k = 1; k < L; k++) A = acc2_add(A, Vs[e + k * C], make_tap2(tap_g(F, k), tap_h(F, k)));
+        acc2_fin(A, d, s);
+      } else {
+        typename P::Acc ad = P::acc_init(Vs[e], tap_g(F, 0));
+        typename P::Acc as = P::acc_init(Vs[e], tap_h(F, 0));
+#pragma unroll
+        for (int k = 1; k < L; k++) {
+          ad = P::acc_add(ad, Vs[e + k * C], tap_g(F, k));
+          as = P::acc_add(as, Vs[e + k * C], tap_h(F, k));
+        }
+        d = P::acc_fin(ad);
+        s = P::acc_fin(as);
+      }
+      emit((r0 + c) + (m0 + row) * d0, s, d);
+    }
+    __syncthreads();  // this stage is refilled two tiles later
+  }
+}
+
+template <int F, class P, class S>
+__device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, int64_t N, int J,
+                           typename P::V* tA, typename P::V* tB) {
+  using V = typename P::V;
+  for (int l = 0; l < J; l++) {
+    V* dst = (l & 1) ? tB : tA;
+    typename P::T* dd_out = det + (int64_t)l * N;
+    auto emit = [&](int64_t i, V s, V d) {
+      dd_out[i] = P::st(d);
+      if (l == J - 1) sJ[i] = P::st(s);
+      else dst[i] = s;
+    };
+    if (l == 0) bfwd_level_tiled<F, P, S>(x, N, 0, emit);
+    else bfwd_level_tiled<F, P, V>((l & 1) ? tA : tB, N, l, emit);
+  }
 }
 
 // Inverse MODWT by tiles of the row view: level l splits the sequence into
