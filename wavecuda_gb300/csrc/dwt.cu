@@ -76,9 +76,62 @@ __device__ __forceinline__ void st2(V* p, V a, V b) {
   }
 }
 
+// Tap pairs of the packed double-float dot products (empty for the other
+// policies), loaded once at the start of a kernel from constant memory:
+// forward (h_j, g_j); inverse (h_2j, h_2j+1) and (g_2j, g_2j+1), each split
+// as make_tap2 does.  Loaded values stay in registers (or constant-bank
+// operands) for the whole kernel; pairs built from immediates would be
+// rebuilt by two moves before every use.
+struct alignas(8) TapPairF {
+  float ch[2], nch[2], ncl[2];
+};
+constexpr TapPairF tap_pair_f(double c0, double c1) {
+  const float h0 = (float)c0, h1 = (float)c1;
+  const float l0 = (float)(c0 - (double)h0), l1 = (float)(c1 - (double)h1);
+  return {{h0, h1}, {-h0, -h1}, {-l0, -l1}};
+}
+struct DwtTapTable {
+  TapPairF f[8], ih[4], ig[4];
+};
+constexpr DwtTapTable dwt_tap_table(int F) {
+  DwtTapTable t{};
+  for (int j = 0; j < filter_len(F); j++) t.f[j] = tap_pair_f(tap_h(F, j), tap_g(F, j));
+  for (int j = 0; j < filter_len(F) / 2; j++) {
+    t.ih[j] = tap_pair_f(tap_h(F, 2 * j), tap_h(F, 2 * j + 1));
+    t.ig[j] = tap_pair_f(tap_g(F, 2 * j), tap_g(F, 2 * j + 1));
+  }
+  return t;
+}
+__constant__ DwtTapTable kDwtTaps[5] = {DwtTapTable{}, dwt_tap_table(1), dwt_tap_table(2),
+                                        dwt_tap_table(3), dwt_tap_table(4)};
+
+__device__ __forceinline__ tap2 load_tap2(const TapPairF& t) {
+  return {*reinterpret_cast<const f32x2*>(t.ch), *reinterpret_cast<const f32x2*>(t.nch),
+          *reinterpret_cast<const f32x2*>(t.ncl)};
+}
+
+template <int F, class P>
+struct PairTaps {
+  __device__ __forceinline__ void init() {}
+};
+template <int F>
+struct PairTaps<F, PDD> {
+  static constexpr int L = filter_len(F);
+  tap2 f[L], ih[L / 2], ig[L / 2];
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int j = 0; j < L; j++) f[j] = load_tap2(kDwtTaps[F].f[j]);
+#pragma unroll
+    for (int j = 0; j < L / 2; j++) {
+      ih[j] = load_tap2(kDwtTaps[F].ih[j]);
+      ig[j] = load_tap2(kDwtTaps[F].ig[j]);
+    }
+  }
+};
+
 template <int F, class P>
 __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V& s,
-                                         typename P::V& d) {
+                                         typename P::V& d, const PairTaps<F, P>& tp) {
   using V = typename P::V;
   constexpr int L = filter_len(F);
   V v[L];
@@ -89,9 +142,9 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
     d = haar_dif<P>(v[0], v[1]);
   } else if constexpr (std::is_same<P, PDD>::value) {
     // s in lane 0, d in lane 1: the same operations as below, packed.
-    dd_acc2 A = acc2_init(v[0], make_tap2(tap_h(F, 0), tap_g(F, 0)));
+    dd_acc2 A = acc2_init(v[0], tp.f[0]);
 #pragma unroll
-    for (int j = 1; j < L; j++) A = acc2_add(A, v[j], make_tap2(tap_h(F, j), tap_g(F, j)));
+    for (int j = 1; j < L; j++) A = acc2_add(A, v[j], tp.f[j]);
     acc2_fin(A, s, d);
   } else {
     typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
@@ -110,19 +163,20 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
 // (sv/dv in ascending j), taps in descending j as daub4.cpp:58-88.
 template <int F, class P>
 __device__ __forceinline__ void inv_pair(const typename P::V* sv, const typename P::V* dv,
-                                         typename P::V& e, typename P::V& o) {
+                                         typename P::V& e, typename P::V& o,
+                                         const PairTaps<F, P>& tp) {
   constexpr int HH = filter_len(F) / 2;
   if constexpr (F == 1) {
     e = haar_sum<P>(sv[0], dv[0]);
     o = haar_dif<P>(sv[0], dv[0]);
   } else if constexpr (std::is_same<P, PDD>::value) {
     // e in lane 0, o in lane 1: the same operations as below, packed.
-    dd_acc2 A = acc2_init(sv[HH - 1], make_tap2(tap_h(F, 2 * (HH - 1)), tap_h(F, 2 * (HH - 1) + 1)));
-    A = acc2_add(A, dv[HH - 1], make_tap2(tap_g(F, 2 * (HH - 1)), tap_g(F, 2 * (HH - 1) + 1)));
+    dd_acc2 A = acc2_init(sv[HH - 1], tp.ih[HH - 1]);
+    A = acc2_add(A, dv[HH - 1], tp.ig[HH - 1]);
 #pragma unroll
     for (int j = HH - 2; j >= 0; j--) {
-      A = acc2_add(A, sv[j], make_tap2(tap_h(F, 2 * j), tap_h(F, 2 * j + 1)));
-      A = acc2_add(A, dv[j], make_tap2(tap_g(F, 2 * j), tap_g(F, 2 * j + 1)));
+      A = acc2_add(A, sv[j], tp.ih[j]);
+      A = acc2_add(A, dv[j], tp.ig[j]);
     }
     acc2_fin(A, e, o);
   } else {
@@ -156,6 +210,8 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
              typename P::T* __restrict__ coarse, int write_coarse_slots, int bulk,
              unsigned int* status, int64_t tile0) {
   using V = typename P::V;
+  PairTaps<F, P> tp;
+  tp.init();
   using T = typename P::T;
   constexpr int L = filter_len(F);
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -199,7 +255,7 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
     const int dstep = 1 << l, doff = 1 << (l - 1);
     for (int k = threadIdx.x; k < nS; k += blockDim.x) {
       V s, d;
-      fwd_pair<F, P>(src + 2 * k, s, d);
+      fwd_pair<F, P>(src + 2 * k, s, d, tp);
       dst[k] = s;
       if (k < nD) Z[doff + k * dstep] = d;
     }
@@ -253,6 +309,8 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
              int64_t Tt, typename P::T* __restrict__ outp, int64_t ostride,
              InvGeom geo, int bulk, unsigned int* status, int64_t tile0) {
   using V = typename P::V;
+  PairTaps<F, P> tp;
+  tp.init();
   using T = typename P::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -311,7 +369,7 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
         dv[j] = Z[(qr - j) * dstep + doff];
       }
       V e, o;
-      inv_pair<F, P>(sv, dv, e, o);
+      inv_pair<F, P>(sv, dv, e, o, tp);
       st2(dst + 2 * qr + geo.off[l - 1], e, o);
     }
     __syncthreads();
@@ -350,6 +408,8 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
              typename P::T* __restrict__ out, typename P::T* __restrict__ coarse,
              unsigned int* status, int64_t ntiles) {
   using V = typename P::V;
+  PairTaps<F, P> tp;
+  tp.init();
   using T = typename P::T;
   static_assert(sizeof(V) == sizeof(T) || std::is_same<V, T>::value, "in-place staging");
   constexpr int L = filter_len(F);
@@ -408,7 +468,7 @@ dwt_fwd_pipe(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
       const int dstep = 1 << l, doff = 1 << (l - 1);
       for (int k = threadIdx.x; k < nS; k += blockDim.x) {
         V s, d;
-        fwd_pair<F, P>(src + 2 * k, s, d);
+        fwd_pair<F, P>(src + 2 * k, s, d, tp);
         dst[k] = s;
         if (k < nD) Z[doff + k * dstep] = d;
       }
@@ -454,6 +514,8 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
              typename P::T* __restrict__ outp, InvGeom geo, unsigned int* status,
              int64_t ntiles) {
   using V = typename P::V;
+  PairTaps<F, P> tp;
+  tp.init();
   using T = typename P::T;
   constexpr int HH = filter_len(F) / 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -526,7 +588,7 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
           dv[j] = Z[(qr - j) * dstep + doff];
         }
         V e, o;
-        inv_pair<F, P>(sv, dv, e, o);
+        inv_pair<F, P>(sv, dv, e, o, tp);
         st2(dst + 2 * qr + geo.off[l - 1], e, o);
       }
       __syncthreads();
