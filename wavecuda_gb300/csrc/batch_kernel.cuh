@@ -28,9 +28,24 @@
 #include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
+#include "wc_taps2.cuh"
 
 namespace wc {
 namespace {
+
+// (g_k, h_k) tap pairs of the packed double-float MODWT forward level
+// (wc_taps2.cuh).
+struct BatchModwtTaps {
+  TapPairF p[8];
+};
+constexpr BatchModwtTaps batch_modwt_taps(int F) {
+  BatchModwtTaps t{};
+  for (int k = 0; k < filter_len(F); k++) t.p[k] = tap_pair_f(tap_g(F, k), tap_h(F, k));
+  return t;
+}
+__constant__ BatchModwtTaps kBatchModwtTaps[5] = {BatchModwtTaps{}, batch_modwt_taps(1),
+                                                  batch_modwt_taps(2), batch_modwt_taps(3),
+                                                  batch_modwt_taps(4)};
 
 constexpr int BT = 512;               // threads per CTA
 constexpr uint64_t kFrac = (1ull << 52) - 1;
@@ -329,9 +344,9 @@ __device__ void bfwd_level_tiled(const S* src, int64_t N, int l, Emit&& emit) {
         s = haar_sum<P>(Vs[e], Vs[e + C]);
       } else if constexpr (std::is_same<P, PDD>::value) {
         // d in lane 0, s in lane 1: the operations below, packed
-        dd_acc2 A = acc2_init(Vs[e], make_tap2(tap_g(F, 0), tap_h(F, 0)));
+        dd_acc2 A = acc2_init(Vs[e], load_tap2(kBatchModwtTaps[F].p[0]));
 #pragma unroll
-        for (int k = 1; k < L; k++) A = acc2_add(A, Vs[e + k * C], make_tap2(tap_g(F, k), tap_h(F, k)));
+        for (int k = 1; k < L; k++) A = acc2_add(A, Vs[e + k * C], load_tap2(kBatchModwtTaps[F].p[k]));
         acc2_fin(A, d, s);
       } else {
         typename P::Acc ad = P::acc_init(Vs[e], tap_g(F, 0));

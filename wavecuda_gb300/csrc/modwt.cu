@@ -31,11 +31,30 @@
 #include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
+#include "wc_taps2.cuh"
 
 namespace wc {
 namespace {
 
 constexpr int kThreads = 256;
+
+// Tap pairs of the packed double-float paths (wc_taps2.cuh): forward
+// (g_k, h_k); inverse (h_k, h_k) and (g_k, g_k).
+struct ModwtTapTable {
+  TapPairF f[8], h[8], g[8];
+};
+constexpr ModwtTapTable modwt_tap_table(int F) {
+  ModwtTapTable t{};
+  for (int k = 0; k < filter_len(F); k++) {
+    t.f[k] = tap_pair_f(tap_g(F, k), tap_h(F, k));
+    t.h[k] = tap_pair_f(tap_h(F, k), tap_h(F, k));
+    t.g[k] = tap_pair_f(tap_g(F, k), tap_g(F, k));
+  }
+  return t;
+}
+__constant__ ModwtTapTable kModwtTaps[5] = {ModwtTapTable{}, modwt_tap_table(1),
+                                            modwt_tap_table(2), modwt_tap_table(3),
+                                            modwt_tap_table(4)};
 
 // Forward analysis of one output from taps v[k * stride], k < L.
 template <int F, class P>
@@ -47,9 +66,9 @@ __device__ __forceinline__ void fwd_taps(const typename P::V* v, int stride, typ
   } else if constexpr (std::is_same<P, PDD>::value) {
     // d in lane 0, s in lane 1: the same operations as below, packed.
     constexpr int L = filter_len(F);
-    dd_acc2 A = acc2_init(v[0], make_tap2(tap_g(F, 0), tap_h(F, 0)));
+    dd_acc2 A = acc2_init(v[0], load_tap2(kModwtTaps[F].f[0]));
 #pragma unroll
-    for (int k = 1; k < L; k++) A = acc2_add(A, v[k * stride], make_tap2(tap_g(F, k), tap_h(F, k)));
+    for (int k = 1; k < L; k++) A = acc2_add(A, v[k * stride], load_tap2(kModwtTaps[F].f[k]));
     acc2_fin(A, d, s);
   } else {
     constexpr int L = filter_len(F);
@@ -98,7 +117,7 @@ __device__ __forceinline__ void inv_taps2_dd(const dd* S, const dd* D, int strid
 #pragma unroll
   for (int t = 0; t < L; t++) {
     const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
-    const tap2 h = make_tap2(tap_h(F, k), tap_h(F, k)), g = make_tap2(tap_g(F, k), tap_g(F, k));
+    const tap2 h = load_tap2(kModwtTaps[F].h[k]), g = load_tap2(kModwtTaps[F].g[k]);
     const dd* s = S - k * stride;
     const dd* d = D - k * stride;
     if (t == 0) A = acc2_init_xy(s[0], s[1], h);
