@@ -26,6 +26,7 @@
 #include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
+#include "wc_taps2.cuh"
 
 namespace wc {
 namespace {
@@ -77,19 +78,9 @@ __device__ __forceinline__ void st2(V* p, V a, V b) {
 }
 
 // Tap pairs of the packed double-float dot products (empty for the other
-// policies), loaded once at the start of a kernel from constant memory:
-// forward (h_j, g_j); inverse (h_2j, h_2j+1) and (g_2j, g_2j+1), each split
-// as make_tap2 does.  Loaded values stay in registers (or constant-bank
-// operands) for the whole kernel; pairs built from immediates would be
-// rebuilt by two moves before every use.
-struct alignas(8) TapPairF {
-  float ch[2], nch[2], ncl[2];
-};
-constexpr TapPairF tap_pair_f(double c0, double c1) {
-  const float h0 = (float)c0, h1 = (float)c1;
-  const float l0 = (float)(c0 - (double)h0), l1 = (float)(c1 - (double)h1);
-  return {{h0, h1}, {-h0, -h1}, {-l0, -l1}};
-}
+// policies), loaded once at the start of a kernel from constant memory
+// (wc_taps2.cuh): forward (h_j, g_j); inverse (h_2j, h_2j+1) and
+// (g_2j, g_2j+1).
 struct DwtTapTable {
   TapPairF f[8], ih[4], ig[4];
 };
@@ -104,11 +95,6 @@ constexpr DwtTapTable dwt_tap_table(int F) {
 }
 __constant__ DwtTapTable kDwtTaps[5] = {DwtTapTable{}, dwt_tap_table(1), dwt_tap_table(2),
                                         dwt_tap_table(3), dwt_tap_table(4)};
-
-__device__ __forceinline__ tap2 load_tap2(const TapPairF& t) {
-  return {*reinterpret_cast<const f32x2*>(t.ch), *reinterpret_cast<const f32x2*>(t.nch),
-          *reinterpret_cast<const f32x2*>(t.ncl)};
-}
 
 template <int F, class P>
 struct PairTaps {
