@@ -286,7 +286,36 @@ dwt_fwd_pass(const typename P::T* __restrict__ in, int64_t N, int G, int64_t Tt,
 struct InvGeom {
   int need[24];  // left halo at level l (coefficients)
   int off[24];   // buffer offset of level l
+  int offmax;    // max over l of off[l]
 };
+
+// Shared memory of an inverse pass, in order: the staged interleaved range
+// [t0 - H, t0 + Tt) (W = Tt + H values of T; two buffers in the pipelined
+// kernel), its details de-interleaved per level (D, W values of V), and the
+// scaling values of the even (SA) and odd (SB) levels.  D holds level l's
+// details d_l[i] = staged[2^(l-1) + i*2^l], i < W >> l, at offset
+// W - (W >> (l-1)): the level loops then read consecutive details from
+// consecutive addresses instead of at stride 2^l (a 2^l-way bank conflict
+// up to 32-way).
+__host__ __device__ inline int64_t inv_sa_len(const InvGeom& g, int64_t Tt) {
+  return Tt + 2 * g.off[0] + 16;
+}
+__host__ __device__ inline int64_t inv_sb_len(const InvGeom& g, int64_t Tt) {
+  return Tt / 2 + 2 * g.offmax + 16;
+}
+
+// Splits the staged details into D (all levels 1..G; the level-G scaling
+// slots, m % 2^G == 0, are skipped), converting them to V.
+template <class P, class Get>
+__device__ __forceinline__ void deinterleave(typename P::V* D, int W, int G, Get&& get) {
+  const int gmask = (1 << G) - 1;
+  for (int m = threadIdx.x; m < W; m += blockDim.x) {
+    if (m & gmask) {
+      const int l = __ffs(m);
+      D[W - (W >> (l - 1)) + (m >> l)] = P::ld(get(m));
+    }
+  }
+}
 
 template <int F, class P>
 __global__ void __launch_bounds__(kThreads)
@@ -301,9 +330,13 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   const int64_t H = (int64_t)geo.need[G] << G;  // left halo of the staged array
-  V* Z = reinterpret_cast<V*>(smem_raw);
-  V* SA = Z + pad16<V>(Tt + H);
-  V* SB = SA + pad16<V>(Tt + 2 * geo.off[0] + 16);
+  const int W = (int)(Tt + H);
+  // D first; the staged range Z is dead once split into D, so SA and SB
+  // reuse its space.
+  V* D = reinterpret_cast<V*>(smem_raw);
+  T* Z = reinterpret_cast<T*>(D + pad16<V>(W));
+  V* SA = reinterpret_cast<V*>(Z);
+  V* SB = SA + pad16<V>(inv_sa_len(geo, Tt));
   const int64_t t0 = (tile0 + (int64_t)blockIdx.x) * Tt;
 
   if (bulk & 1) {
@@ -317,19 +350,16 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
         bulk_g2s(Z, det + (t0 - H), (uint32_t)((Tt + H) * sizeof(T)), &bar);
       } else {
         bulk_g2s(Z, det + (N - H), (uint32_t)(H * sizeof(T)), &bar);
-        bulk_g2s(reinterpret_cast<T*>(Z) + H, det + t0, (uint32_t)(Tt * sizeof(T)), &bar);
+        bulk_g2s(Z + H, det + t0, (uint32_t)(Tt * sizeof(T)), &bar);
       }
     }
     const bool ok = mbar_wait(&bar, 0, status);
     if (__syncthreads_or(!ok)) return;
-    if constexpr (!std::is_same<T, V>::value) {
-      for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
-        Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
-    }
+    deinterleave<P>(D, W, G, [&](int m) { return Z[m]; });
   } else {
-    for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
-      Z[m] = P::ld(det[wrap(t0 - H + m, N) * S]);
+    deinterleave<P>(D, W, G, [&](int m) { return det[wrap(t0 - H + m, N) * S]; });
   }
+  __syncthreads();  // Z is read; SA and SB overwrite it
   {
     const int64_t NG = N >> G, q0 = t0 >> G;
     const int cnt = (int)(Tt >> G) + geo.need[G];
@@ -344,7 +374,7 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
     V* dst = (l & 1) ? SA : SB;
     const int P_l = (geo.need[l - 1] + 1) >> 1;
     const int nq = (int)(Tt >> l) + P_l;
-    const int dstep = 1 << l, doff = (1 << (l - 1)) + (int)H;
+    const V* Dl = D + (W - (W >> (l - 1))) + (int)(H >> l);
     for (int k = threadIdx.x; k < nq; k += blockDim.x) {
       const int qr = k - P_l;  // q - q0
       constexpr int HH = filter_len(F) / 2;
@@ -352,7 +382,7 @@ dwt_inv_pass(const typename P::T* __restrict__ coarse, int64_t cstride,
 #pragma unroll
       for (int j = 0; j < HH; j++) {
         sv[j] = src[qr - j + geo.off[l]];
-        dv[j] = Z[(qr - j) * dstep + doff];
+        dv[j] = Dl[qr - j];
       }
       V e, o;
       inv_pair<F, P>(sv, dv, e, o, tp);
@@ -507,10 +537,12 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar[2];
   const int64_t H = (int64_t)geo.need[G] << G;
-  V* const Z0 = reinterpret_cast<V*>(smem_raw);
-  V* const Z1 = Z0 + pad16<V>(Tt + H);
-  V* SA = Z1 + pad16<V>(Tt + H);
-  V* SB = SA + pad16<V>(Tt + 2 * geo.off[0] + 16);
+  const int W = (int)(Tt + H);
+  T* const Z0 = reinterpret_cast<T*>(smem_raw);
+  T* const Z1 = Z0 + pad16<T>(W);
+  V* const D = reinterpret_cast<V*>(Z1 + pad16<T>(W));
+  V* SA = D + pad16<V>(W);
+  V* SB = SA + pad16<V>(inv_sa_len(geo, Tt));
   int64_t tile = blockIdx.x;
   if (tile >= ntiles) return;
   if (threadIdx.x == 0) {
@@ -520,7 +552,7 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
   __syncthreads();
   auto issue = [&](int64_t tl, int b) {
     const int64_t t0 = tl * Tt;
-    T* dst = reinterpret_cast<T*>(b ? Z1 : Z0);
+    T* dst = b ? Z1 : Z0;
     mbar_expect_tx(&bar[b], (uint32_t)((Tt + H) * sizeof(T)));
     if (t0 >= H) {
       bulk_g2s(dst, det + (t0 - H), (uint32_t)((Tt + H) * sizeof(T)), &bar[b]);
@@ -546,11 +578,8 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
       if (threadIdx.x == 0) bulk_wait_read();
       return;
     }
-    V* Z = b ? Z1 : Z0;
-    if constexpr (!std::is_same<T, V>::value) {
-      for (int m = threadIdx.x; m < (int)(Tt + H); m += blockDim.x)
-        Z[m] = P::ld(reinterpret_cast<const T*>(Z)[m]);
-    }
+    const T* Z = b ? Z1 : Z0;
+    deinterleave<P>(D, W, G, [&](int m) { return Z[m]; });
     {
       const int64_t q0 = t0 >> G;
       const int cnt = (int)(Tt >> G) + geo.need[G];
@@ -564,14 +593,14 @@ dwt_inv_pipe(const typename P::T* __restrict__ coarse, int64_t cstride,
       V* dst = (l & 1) ? SA : SB;
       const int P_l = (geo.need[l - 1] + 1) >> 1;
       const int nq = (int)(Tt >> l) + P_l;
-      const int dstep = 1 << l, doff = (1 << (l - 1)) + (int)H;
+      const V* Dl = D + (W - (W >> (l - 1))) + (int)(H >> l);
       for (int k = threadIdx.x; k < nq; k += blockDim.x) {
         const int qr = k - P_l;
         V sv[HH], dv[HH];
 #pragma unroll
         for (int j = 0; j < HH; j++) {
           sv[j] = src[qr - j + geo.off[l]];
-          dv[j] = Z[(qr - j) * dstep + doff];
+          dv[j] = Dl[qr - j];
         }
         V e, o;
         inv_pair<F, P>(sv, dv, e, o, tp);
@@ -621,6 +650,8 @@ InvGeom inv_geom(int L, int G) {
   for (int l = 1; l <= G; l++) g.need[l] = (g.need[l - 1] + 1) / 2 + L / 2 - 1;
   g.off[G] = g.need[G];
   for (int l = 0; l < G; l++) g.off[l] = 2 * ((g.need[l] + 1) / 2);
+  g.offmax = 0;
+  for (int l = 0; l <= G; l++) g.offmax = std::max(g.offmax, g.off[l]);
   return g;
 }
 
@@ -629,7 +660,11 @@ size_t inv_smem(int L, int G, int64_t Tt) {
   InvGeom g = inv_geom(L, G);
   int64_t H = (int64_t)g.need[G] << G;
   using V = typename P::V;
-  return sizeof(V) * (size_t)(pad16<V>(Tt + H) + 2 * pad16<V>(Tt + 2 * g.off[0] + 16));
+  using T = typename P::T;
+  const size_t staged = sizeof(T) * (size_t)pad16<T>(Tt + H);
+  const size_t scal =
+      sizeof(V) * (size_t)(pad16<V>(inv_sa_len(g, Tt)) + pad16<V>(inv_sb_len(g, Tt)));
+  return sizeof(V) * (size_t)pad16<V>(Tt + H) + std::max(staged, scal);
 }
 
 template <class P>
@@ -643,8 +678,8 @@ std::vector<PassPlan> plan_passes(int64_t n, int J, int F) {
   while (l < J) {
     const int64_t Tt = std::min(N, TT);
     int G = std::min(J - l, (Tt == N) ? 30 : gmax);
-    while ((((int64_t)1 << G) > Tt) ||
-           fwd_smem<P>(L, G, Tt) > kSmemBudget || inv_smem<P>(L, G, Tt) > kSmemBudget)
+    while (G > 1 && ((((int64_t)1 << G) > Tt) || fwd_smem<P>(L, G, Tt) > kSmemBudget ||
+                     inv_smem<P>(L, G, Tt) > kSmemBudget))
       G--;
     plan.push_back({N, S, Tt, G});
     N >>= G;
@@ -711,7 +746,10 @@ size_t inv_pipe_smem(int L, int G, int64_t Tt) {
   InvGeom g = inv_geom(L, G);
   const int64_t H = (int64_t)g.need[G] << G;
   using V = typename P::V;
-  return sizeof(V) * (size_t)(2 * pad16<V>(Tt + H) + 2 * pad16<V>(Tt + 2 * g.off[0] + 16));
+  using T = typename P::T;
+  return 2 * sizeof(T) * (size_t)pad16<T>(Tt + H) +
+         sizeof(V) * (size_t)(pad16<V>(Tt + H) + pad16<V>(inv_sa_len(g, Tt)) +
+                              pad16<V>(inv_sb_len(g, Tt)));
 }
 
 constexpr size_t kPipeSmemMax = 200 * 1024;
