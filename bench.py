@@ -260,7 +260,8 @@ def ours(args):
     maxJ_mod = 12
     bufs = (wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n * 2 * maxJ_mod), wc.DeviceBuffer(8 * n))
     x = signals.roofline_input(n, seed=1 + dist.rank)
-    bufs[0].upload(x)
+    esz = 4 if prec == 2 else 8  # bytes per sample in HBM (FP32 data for WC_F32)
+    bufs[0].upload(x.astype(np.float32) if prec == 2 else x)
 
     # Autotune the DWT first-pass tiling (setup, not timed).
     tiling = {}
@@ -288,12 +289,12 @@ def ours(args):
     value = args.steps * n * dist.world / (ms / 1e3) / 1e9
 
     # correctness guard on the timed output: perfect reconstruction
-    r = bufs[2].download(np.float64, n)
+    r = bufs[2].download(np.float32 if prec == 2 else np.float64, n).astype(np.float64)
     pr_err = float(np.max(np.abs(r - x)) / np.max(np.abs(x)))
 
     # dominant kernel and its live per-launch time
     dom = max(prof, key=lambda p: p[2]) if prof else ("", 1, ms)
-    dom_bytes = algorithmic_bytes(dom[0], n, J, 8)
+    dom_bytes = algorithmic_bytes(dom[0], n, J, esz)
     dom_avg_s = dom[2] / dom[1] / 1e3
     achieved = dom_bytes / dom_avg_s / 1e9 if dom_bytes else None
     traffic = None
@@ -304,7 +305,7 @@ def ours(args):
                 "peak_source": hbm_src, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                 "bytes_per_launch": dom_bytes, "avg_launch_ms": dom_avg_s * 1e3,
-                "step_frac": step_bytes(0, n, J, 8) * args.steps / (ms / 1e3) / 1e9 / hbm,
+                "step_frac": step_bytes(0, n, J, esz) * args.steps / (ms / 1e3) / 1e9 / hbm,
                 "kernels": [{"name": p[0], "launches": p[1], "total_ms": round(p[2], 4)}
                             for p in prof]}
 
@@ -344,9 +345,9 @@ def ours(args):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic: iid N(0,1) + 8 sinusoids, seeded",
            "config": {"workload": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.log2n}, J={J}, "
-                                  f"FP64 data, {PREC[prec]} arithmetic",
+                                  f"{'FP32' if prec == 2 else 'FP64'} data, {PREC[prec]} arithmetic",
                       "n": n, "levels": J, "filter": FILTERS[filt], "precision": PREC[prec],
-                      "l2": "inputs (512 MiB) larger than L2; no flush",
+                      "l2": f"inputs ({n * esz >> 20} MiB) larger than L2; no flush",
                       "parallelism": f"replicas x{dist.world}"},
            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
            "pr_err": pr_err}
