@@ -265,6 +265,35 @@ WC_API int wc_median_mad_device(const double* data, int64_t n, double* median, d
  * Computed in parallel; synchronous; the sum is returned on the host. */
 WC_API int wc_sequential_sum_device(const double* terms, int64_t n, double* sum, void* stream);
 
+/* ---- coefficient extraction and formatting (R/rplotting.R:10-46,
+ * R/rfunctions.R:925-1004), for large n on the device.  ttype 0 DWT
+ * (interleaved, len values) or 1 time-ordered MODWT (2*nlevels*len values);
+ * len a power of 2, 1 <= nlevels <= log2(len). */
+
+/* getCoeffLevel(xw, level, coeffType) (rplotting.R:10-46): the 1-based
+ * indices of the coefficients of `level` (1..nlevels); coeff_type 1 details
+ * ("d"), 0 scaling ("s", DWT: level == nlevels only).  DWT: 2^(level-1)*d + 1
+ * step 2^level; MODWT: 1..len whatever the level, as the reference returns.
+ * Host arithmetic; idx may be NULL to query *count. */
+WC_API int wc_coeff_level_indices(int64_t len, int nlevels, int ttype, int level, int coeff_type,
+                                  int64_t* idx, int64_t capacity, int64_t* count);
+
+/* Rows of WSTtoDT(xw, scaling, forPlotting = FALSE) (rfunctions.R:925-1004):
+ * len (DWT) or 2*nlevels*len (MODWT) with scaling != 0, and without the
+ * scaling rows len - len/2^nlevels or nlevels*len. */
+WC_API int wc_wst_table_rows(int64_t len, int nlevels, int ttype, int scaling, int64_t* rows);
+
+/* The WSTtoDT columns, in its row order: W (the coefficient), Level,
+ * Translate and CoeffType (0 "s", 1 "d"); any column pointer may be NULL.
+ * The per-level min/max placeholder rows of forPlotting = TRUE are not
+ * produced.  Device pointers, enqueued on `stream`. */
+WC_API int wc_wst_table_device(const double* w, int64_t len, int nlevels, int ttype, int scaling,
+                               double* W, int32_t* level, double* translate, uint8_t* type,
+                               void* stream);
+/* The same with host arrays (copies in and out included; synchronous). */
+WC_API int wc_wst_table(const double* w, int64_t len, int nlevels, int ttype, int scaling,
+                        double* W, int32_t* level, double* translate, uint8_t* type);
+
 /* ---- differentiation (no counterpart in the reference; backward calls for
  * gradient-based threshold tuning).  FP64 device vectors; `sense` names the
  * operator whose adjoint is applied (1 = the forward transform, 0 = the

@@ -297,3 +297,52 @@ class Reference:
 
 def reference_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+# ---------------------------------------------------------------------------
+# Coefficient extraction and formatting (R code of the reference, restated
+# step by step in numpy; R is not available here, so these follow the R
+# source line by line rather than a compiled reference).
+
+def coeff_level(n, nlevels, ttype, level, coeff_type="d"):
+    """getCoeffLevel (R/rplotting.R:10-46): 1-based indices."""
+    if level <= 0 or level > nlevels:
+        raise ValueError("Integer level expected")
+    d_bool = 1 if coeff_type == "d" else 0
+    if ttype == DWT:
+        if not d_bool and level != nlevels:
+            raise ValueError("stopifnot(level == xw$nlevels)")
+        start, gap = 2 ** (level - 1) * d_bool + 1, 2 ** level
+    else:
+        start, gap = 1, 1
+    return np.arange(start, n + 1, gap, dtype=np.int64)          # seq(start, n, by = gap)
+
+
+def wst_to_dt(w, n, nlevels, ttype, scaling=True):
+    """WSTtoDT(Xwav, scaling, forPlotting = FALSE) (R/rfunctions.R:925-1004):
+    columns W, CoeffType, Level, Translate in row order (without data.table)."""
+    J = nlevels
+    w = np.asarray(w, dtype=np.float64)
+    if ttype == DWT:
+        i1 = np.arange(1, n + 1)
+        ctype = np.where(i1 % (2 ** J) == 1, "s", "d")             # label.detail.scaling
+        level = np.ones(n, dtype=np.int64)                          # rep(1, len)
+        translate = np.repeat(np.arange(0.5, n / 2, 1.0), 2)        # rep(seq(0.5, len/2, 1), each = 2)
+        if J > 1:
+            for l in range(2, J + 1):
+                rows = coeff_level(n, J, DWT, l, "d") - 1
+                level[rows] = l
+                translates = np.arange(2.0 ** (l - 2), n / 2 + 1e-9, 2.0 ** (l - 1))
+                translate[rows] = translates
+            rows = coeff_level(n, J, DWT, J, "s") - 1                # l == nlevels after the loop
+            level[rows] = J
+            translate[rows] = translates
+        W = w[:n].copy()
+    else:
+        W = w[:2 * J * n].copy()
+        ctype = np.tile(np.repeat(np.array(["s", "d"]), n), J)
+        level = np.repeat(np.arange(1, J + 1), 2 * n)
+        translate = np.tile(np.arange(1, n + 1, dtype=np.float64), 2 * J)
+    keep = np.ones(W.size, dtype=bool) if scaling else (ctype == "d")
+    return {"W": W[keep], "CoeffType": ctype[keep], "Level": level[keep].astype(np.int64),
+            "Translate": translate[keep]}

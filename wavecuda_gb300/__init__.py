@@ -156,6 +156,14 @@ def lib() -> C.CDLL:
     L.wc_event_record.argtypes = [_vp, _vp]
     L.wc_event_elapsed_ms.argtypes = [_vp, _vp, C.POINTER(C.c_float)]
     L.wc_kernel_launch_count.restype = C.c_int64
+    _i64p = C.POINTER(C.c_int64)
+    L.wc_coeff_level_indices.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, _i64p,
+                                         C.c_int64, _i64p]
+    L.wc_wst_table_rows.argtypes = [C.c_int64, C.c_int, C.c_int, C.c_int, _i64p]
+    L.wc_wst_table_device.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp,
+                                      _vp, _vp]
+    L.wc_wst_table.argtypes = [_dp, C.c_int64, C.c_int, C.c_int, C.c_int, _dp,
+                               C.POINTER(C.c_int32), _dp, C.POINTER(C.c_uint8)]
     _lib = L
     return L
 
@@ -392,6 +400,57 @@ def CPUSmooth(xin, nlevels, transform_type, filter, thresh_type, thresh=None, ha
     a = check_smooth_inputs(xin, nlevels, transform_type, filter, thresh_type, thresh, hard_soft,
                             min_level, max_level, tol)
     return _call_smooth("RcpuSmooth", a)
+
+
+def getCoeffLevel(xw: WST, level, coeffType="d"):
+    """getCoeffLevel (R/rplotting.R:10-46): 1-based indices of the
+    coefficients of `level` in xw.w (DWT: 2^(level-1)*[d] + 1 step 2^level;
+    MODWT: 1..len whatever the level, as the reference returns)."""
+    if not isinstance(xw, WST):
+        raise ValueError("WST type required")
+    if level <= 0 or level > xw.nlevels or level != int(level):
+        raise ValueError(f"Integer level expected, between 1 and {xw.nlevels}")
+    if coeffType not in ("d", "s"):
+        raise ValueError("coeffType must be 'd' or 's'")
+    if xw.ttype == "DWT" and coeffType == "s" and level != xw.nlevels:
+        raise ValueError("level == xw$nlevels is not TRUE")
+    L = lib()
+    ttype = DWT if xw.ttype == "DWT" else MODWT
+    cnt = C.c_int64()
+    ct = 1 if coeffType == "d" else 0
+    check(L.wc_coeff_level_indices(xw.len, xw.nlevels, ttype, int(level), ct, None, 0,
+                                   C.byref(cnt)))
+    idx = np.empty(cnt.value, dtype=np.int64)
+    check(L.wc_coeff_level_indices(xw.len, xw.nlevels, ttype, int(level), ct,
+                                   idx.ctypes.data_as(C.POINTER(C.c_int64)), idx.size,
+                                   C.byref(cnt)))
+    return idx
+
+
+def WSTtoDT(xw: WST, scaling=True, forPlotting=False):
+    """WSTtoDT (R/rfunctions.R:925-1004) without data.table: the columns W,
+    CoeffType ("s"/"d"), Level and Translate as numpy arrays, in the
+    reference's row order, computed on the GPU (wc_wst_table).  The plotting
+    rows of forPlotting = TRUE (per-level min/max placeholders) are not
+    provided: plotting is outside this library."""
+    if forPlotting:
+        raise NotImplementedError("forPlotting rows are plotting-only and not provided")
+    if xw.ttype not in ("DWT", "MODWT"):
+        raise ValueError("WSTtoDT takes DWT or MODWT transforms")
+    L = lib()
+    ttype = DWT if xw.ttype == "DWT" else MODWT
+    rows = C.c_int64()
+    check(L.wc_wst_table_rows(xw.len, xw.nlevels, ttype, int(bool(scaling)), C.byref(rows)))
+    n = rows.value
+    W = np.empty(n, dtype=np.float64)
+    lev = np.empty(n, dtype=np.int32)
+    tr = np.empty(n, dtype=np.float64)
+    ty = np.empty(n, dtype=np.uint8)
+    w = np.ascontiguousarray(xw.w, dtype=np.float64)
+    check(L.wc_wst_table(_dptr(w), xw.len, xw.nlevels, ttype, int(bool(scaling)), _dptr(W),
+                         lev.ctypes.data_as(C.POINTER(C.c_int32)), _dptr(tr),
+                         ty.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return {"W": W, "CoeffType": np.where(ty == 1, "d", "s"), "Level": lev, "Translate": tr}
 
 
 def GPUSmooth(xin, nlevels, transform_type, filter, thresh_type, thresh=None, hard_soft="soft",
