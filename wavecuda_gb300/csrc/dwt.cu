@@ -289,10 +289,12 @@ struct InvGeom {
   int offmax;    // max over l of off[l]
 };
 
-// Shared memory of an inverse pass, in order: the staged interleaved range
+// Shared memory of an inverse pass: the staged interleaved range
 // [t0 - H, t0 + Tt) (W = Tt + H values of T; two buffers in the pipelined
 // kernel), its details de-interleaved per level (D, W values of V), and the
-// scaling values of the even (SA) and odd (SB) levels.  D holds level l's
+// scaling values of the even (SA) and odd (SB) levels.  The pipelined kernel
+// keeps the staging buffers, D, SA and SB apart; the per-tile kernel puts D
+// first and SA/SB in the staging space, which is dead once split.  D holds level l's
 // details d_l[i] = staged[2^(l-1) + i*2^l], i < W >> l, at offset
 // W - (W >> (l-1)): the level loops then read consecutive details from
 // consecutive addresses instead of at stride 2^l (a 2^l-way bank conflict
