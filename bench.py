@@ -334,6 +334,9 @@ def ours(args):
     for _ in range(args.steps):
         e2e_step()
     t_e2e = dist.max(time.perf_counter() - t0)
+    # reconstruction error of one round trip (the timed steps ran in place)
+    hx.array[:] = x
+    e2e_step()
     e2e_err = float(np.max(np.abs(hx.array - x)) / np.max(np.abs(x)))
     e2e = {"value": args.steps * n * dist.world / t_e2e / 1e9, "unit": "Gsamples/s",
            "h2d_bytes_per_step": 2 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,

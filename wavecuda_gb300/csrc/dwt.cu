@@ -96,6 +96,16 @@ constexpr DwtTapTable dwt_tap_table(int F) {
 __constant__ DwtTapTable kDwtTaps[5] = {DwtTapTable{}, dwt_tap_table(1), dwt_tap_table(2),
                                         dwt_tap_table(3), dwt_tap_table(4)};
 
+// max(|c0|, |c1|) with a relative margin of 1e-6 (the sigma bound of the
+// extraction dot products).
+__host__ __device__ constexpr float tap_pair_max(double c0, double c1) {
+  const double a = c0 < 0 ? -c0 : c0, b = c1 < 0 ? -c1 : c1;
+  return (float)((a > b ? a : b) * (1.0 + 1e-6));
+}
+__host__ __device__ constexpr float tap_hg_max(int F, int j) {
+  return tap_pair_max(tap_h(F, j), tap_g(F, j));
+}
+
 template <int F, class P>
 struct PairTaps {
   __device__ __forceinline__ void init() {}
@@ -128,10 +138,15 @@ __device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V
     d = haar_dif<P>(v[0], v[1]);
   } else if constexpr (std::is_same<P, PDD>::value) {
     // s in lane 0, d in lane 1: the same operations as below, packed.
-    dd_acc2 A = acc2_init(v[0], tp.f[0]);
+    // By extraction (wc_dd.cuh); sigma from sum_j |v_j| max(|h_j|, |g_j|).
+    float as = 0.f;
 #pragma unroll
-    for (int j = 1; j < L; j++) A = acc2_add(A, v[j], tp.f[j]);
-    acc2_fin(A, s, d);
+    for (int j = 0; j < L; j++) as = __fmaf_rn(fabsf(v[j].hi), tap_hg_max(F, j), as);
+    const f32x2 sig = extract_sigma(as);
+    dd_accx A = accx_init(v[0], tp.f[0], sig);
+#pragma unroll
+    for (int j = 1; j < L; j++) A = accx_add(A, v[j], tp.f[j], sig);
+    accx_fin(A, s, d);
   } else {
     typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
     typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
@@ -157,14 +172,23 @@ __device__ __forceinline__ void inv_pair(const typename P::V* sv, const typename
     o = haar_dif<P>(sv[0], dv[0]);
   } else if constexpr (std::is_same<P, PDD>::value) {
     // e in lane 0, o in lane 1: the same operations as below, packed.
-    dd_acc2 A = acc2_init(sv[HH - 1], tp.ih[HH - 1]);
-    A = acc2_add(A, dv[HH - 1], tp.ig[HH - 1]);
+    // By extraction (wc_dd.cuh); sigma from the inputs' |.| times the
+    // larger of the two lanes' taps.
+    float as = 0.f;
+#pragma unroll
+    for (int j = 0; j < HH; j++) {
+      as = __fmaf_rn(fabsf(sv[j].hi), tap_pair_max(tap_h(F, 2 * j), tap_h(F, 2 * j + 1)), as);
+      as = __fmaf_rn(fabsf(dv[j].hi), tap_pair_max(tap_g(F, 2 * j), tap_g(F, 2 * j + 1)), as);
+    }
+    const f32x2 sig = extract_sigma(as);
+    dd_accx A = accx_init(sv[HH - 1], tp.ih[HH - 1], sig);
+    A = accx_add(A, dv[HH - 1], tp.ig[HH - 1], sig);
 #pragma unroll
     for (int j = HH - 2; j >= 0; j--) {
-      A = acc2_add(A, sv[j], tp.ih[j]);
-      A = acc2_add(A, dv[j], tp.ig[j]);
+      A = accx_add(A, sv[j], tp.ih[j], sig);
+      A = accx_add(A, dv[j], tp.ig[j], sig);
     }
-    acc2_fin(A, e, o);
+    accx_fin(A, e, o);
   } else {
     typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
     typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));

@@ -274,4 +274,57 @@ __device__ __forceinline__ dd_acc2 acc2_add_xy(dd_acc2 A, dd a0, dd a1, const ta
   return {s, x2_add(A.ne, x2_sub(npe, t))};
 }
 
+// ---------------------------------------------------------------------------
+// Two dot products by extraction (ExtractScalar of Rump, Ogita and Oishi,
+// "Accurate floating-point summation, part I: faithful rounding", SIAM J.
+// Sci. Comput. 31(1), 2008).  sigma is a power of two with
+// sigma >= 2 * sum_k |a_k.hi * c_k| over both lanes' taps.  Then
+// t = fl(sigma + a.hi*ch) (one FMA) lies in [sigma/2, 3 sigma/2], so
+// q = t - sigma is exact (Sterbenz) and a multiple of 2^-24 sigma, and every
+// partial sum of the q's stays below sigma in magnitude: the high parts add
+// up in FP32 without rounding.  The residual a.hi*ch - q (one FMA, rounded
+// once, |residual| <= 2^-24 sigma) and the cross terms a.hi*cl + a.lo*ch go
+// into the error float, so the error is a few units of 2^-48 sigma (at most
+// about 2^-46 of sum |a*c| per dot product).  Seven packed instructions per
+// tap against acc2_add's twelve.
+struct dd_accx {
+  f32x2 S, ne;  // exact sum of the extracted high parts; negated error sum
+};
+
+// Smallest power of two >= 2 * s (s >= 0; 0 for s == 0), in both lanes.
+__device__ __forceinline__ f32x2 extract_sigma(float s) {
+  const unsigned int b = __float_as_uint(__fmul_rn(s, 2.f));
+  const float sg = __uint_as_float((b + 0x7FFFFFu) & 0xFF800000u);
+  return x2_pack(sg, sg);
+}
+
+__device__ __forceinline__ dd_accx accx_init(f32x2 ah, f32x2 al, const tap2& c, f32x2 sig) {
+  const f32x2 q = x2_sub(x2_fma(ah, c.ch, sig), sig);
+  f32x2 ne = x2_fma(ah, c.nch, q);  // q - a.hi*ch
+  ne = x2_fma(ah, c.ncl, ne);
+  ne = x2_fma(al, c.nch, ne);
+  return {q, ne};
+}
+
+__device__ __forceinline__ dd_accx accx_add(dd_accx A, f32x2 ah, f32x2 al, const tap2& c,
+                                            f32x2 sig) {
+  const f32x2 q = x2_sub(x2_fma(ah, c.ch, sig), sig);
+  const f32x2 u = x2_fma(ah, c.nch, q);
+  f32x2 ne = x2_fma(ah, c.ncl, A.ne);
+  ne = x2_fma(al, c.nch, ne);
+  return {x2_add(A.S, q), x2_add(ne, u)};
+}
+
+// Same input in both lanes (two filters applied to one window).
+__device__ __forceinline__ dd_accx accx_init(dd a, const tap2& c, f32x2 sig) {
+  return accx_init(x2_pack(a.hi, a.hi), x2_pack(a.lo, a.lo), c, sig);
+}
+__device__ __forceinline__ dd_accx accx_add(dd_accx A, dd a, const tap2& c, f32x2 sig) {
+  return accx_add(A, x2_pack(a.hi, a.hi), x2_pack(a.lo, a.lo), c, sig);
+}
+
+__device__ __forceinline__ void accx_fin(dd_accx A, dd& r0, dd& r1) {
+  acc2_fin(dd_acc2{A.S, A.ne}, r0, r1);
+}
+
 }  // namespace wc
