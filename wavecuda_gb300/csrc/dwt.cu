@@ -96,16 +96,6 @@ constexpr DwtTapTable dwt_tap_table(int F) {
 __constant__ DwtTapTable kDwtTaps[5] = {DwtTapTable{}, dwt_tap_table(1), dwt_tap_table(2),
                                         dwt_tap_table(3), dwt_tap_table(4)};
 
-// max(|c0|, |c1|) with a relative margin of 1e-6 (the sigma bound of the
-// extraction dot products).
-__host__ __device__ constexpr float tap_pair_max(double c0, double c1) {
-  const double a = c0 < 0 ? -c0 : c0, b = c1 < 0 ? -c1 : c1;
-  return (float)((a > b ? a : b) * (1.0 + 1e-6));
-}
-__host__ __device__ constexpr float tap_hg_max(int F, int j) {
-  return tap_pair_max(tap_h(F, j), tap_g(F, j));
-}
-
 template <int F, class P>
 struct PairTaps {
   __device__ __forceinline__ void init() {}

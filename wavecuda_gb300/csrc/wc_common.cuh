@@ -40,6 +40,16 @@ __host__ __device__ constexpr double tap_g(int F, int k) {
   return (k & 1) ? -tap_h(F, filter_len(F) - 1 - k) : tap_h(F, filter_len(F) - 1 - k);
 }
 
+// max(|c0|, |c1|) with a relative margin of 1e-6 (the sigma bound of the
+// extraction dot products).
+__host__ __device__ constexpr float tap_pair_max(double c0, double c1) {
+  const double a = c0 < 0 ? -c0 : c0, b = c1 < 0 ? -c1 : c1;
+  return (float)((a > b ? a : b) * (1.0 + 1e-6));
+}
+__host__ __device__ constexpr float tap_hg_max(int F, int j) {
+  return tap_pair_max(tap_h(F, j), tap_g(F, j));
+}
+
 constexpr double kInvR2 = 0.70710678118654752440;   // haarcoeffs.h:4
 constexpr double kHInvR2 = 0.35355339059327376220;  // haarcoeffs.h:5
 
