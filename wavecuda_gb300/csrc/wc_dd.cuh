@@ -11,7 +11,8 @@
 // SIAM J. Sci. Comput. 26(6), 2005): the high parts of the products are
 // summed with TwoSum, every rounding error (product errors, cross terms
 // xh*cl + xl*ch, sum errors) goes into one float, and the pair is
-// renormalised once per output.  About 12 FP32 instructions per tap.
+// renormalised once per output.  About 12 FP32 instructions per tap.  The
+// DWT passes use the cheaper extraction scheme at the end of this file.
 //
 // Conversions never touch the FP64 pipe.  A double x = (-1)^s 2^e 1.f is
 // split by bit manipulation: hi keeps the top 23 fraction bits (exact,
@@ -284,9 +285,10 @@ __device__ __forceinline__ dd_acc2 acc2_add_xy(dd_acc2 A, dd a0, dd a1, const ta
 // partial sum of the q's stays below sigma in magnitude: the high parts add
 // up in FP32 without rounding.  The residual a.hi*ch - q (one FMA, rounded
 // once, |residual| <= 2^-24 sigma) and the cross terms a.hi*cl + a.lo*ch go
-// into the error float, so the error is a few units of 2^-48 sigma (at most
-// about 2^-46 of sum |a*c| per dot product).  Seven packed instructions per
-// tap against acc2_add's twelve.
+// into the error float, so the error is a few units of 2^-48 sigma: over
+// random windows of an exact-rational emulation of these steps, a median of
+// 1.2e-14 and a worst case of 2.6e-13 of sum |a*c| (Dot2: 1.4e-15 and
+// 1.3e-14).  Seven packed instructions per tap against acc2_add's twelve.
 struct dd_accx {
   f32x2 S, ne;  // exact sum of the extracted high parts; negated error sum
 };
