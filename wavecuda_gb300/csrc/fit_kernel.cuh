@@ -119,6 +119,18 @@ __device__ void badj_modwt(const typename P::V* g, const typename P::T* det, int
         if constexpr (F == 1) {
           d = haar_dif<P>(v[u][0], v[u][1]);
           s = haar_sum<P>(v[u][0], v[u][1]);
+        } else if constexpr (std::is_same<P, PDD>::value) {
+          // The cotangents only reach FP32 partial sums of the gradient, so
+          // in double-float mode the adjoint sweep runs in FP32 on the high
+          // parts (a plain FP32 dot product per output).
+          float fd = 0.f, fs = 0.f;
+#pragma unroll
+          for (int k = 0; k < L; k++) {
+            fd = __fmaf_rn(v[u][k].hi, (float)tap_g(F, k), fd);
+            fs = __fmaf_rn(v[u][k].hi, (float)tap_h(F, k), fs);
+          }
+          d = dd{fd, 0.f};
+          s = dd{fs, 0.f};
         } else {
           typename P::Acc ad = P::acc_init(v[u][0], tap_g(F, 0));
           typename P::Acc as = P::acc_init(v[u][0], tap_h(F, 0));
