@@ -1411,7 +1411,7 @@ extern "C" int wc_tune_dwt(int filter, int precision, int log2n, float* best_ms)
   const int tiles8[3] = {1024, 2048, 4096}, tiles4[3] = {2048, 4096, 8192};
   for (int ti = 0; ti < 3; ti++) {
     const int tile = (precision == WC_F32) ? tiles4[ti] : tiles8[ti];
-    for (int g : {gm - 2, gm - 1, gm}) {
+    for (int g : {gm - 2, gm - 1, gm, gm + 1}) {
       if (g < 1 || (1 << g) > tile) continue;
       for (int th : {256, 512})
         for (int pp : {1, 0}) cand.push_back(TileCfg{tile, g, th, pp});
