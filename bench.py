@@ -183,6 +183,21 @@ def algorithmic_bytes(kernel: str, n: int, J: int, esize: int) -> float:
     return 0.0
 
 
+def fp64_ops_per_sample(ttype: int, filt: int, J: int) -> float:
+    """Separately rounded FP64 operations per sample of a forward+inverse
+    transform in the reference's formulas (what the exact mode issues).
+    DWT: a level of N inputs costs N/2 pairs of 2L mul + 2(L-1) add forward
+    (daub4.cpp:20-56) and as many inverse (Haar: 2 + 2 per pair); the levels
+    see 2n(1 - 2^-J) inputs in all.  MODWT (daub4.cpp:561-589): per sample
+    and level 2L mul + 2(L-1) add forward, 2L + 1 mul + 2L - 1 add inverse
+    (Haar 4 + 4)."""
+    L = 2 * filt
+    if ttype == 0:
+        per_input = 4.0 if filt == 1 else 2.0 * (2 * L - 1)   # fwd + inv
+        return 2.0 * (1 - 2.0 ** -J) * per_input
+    return J * (8.0 if filt == 1 else 8.0 * L - 2)
+
+
 def step_bytes(ttype: int, n: int, J: int, esize: int) -> float:
     if ttype == 0:
         return 4.0 * n * esize                         # fwd 2n + inv 2n
@@ -343,6 +358,23 @@ def ours(args):
            "api": "RgpuTransform FWD+BWD, pinned host buffers", "pr_err": e2e_err}
     hx.free()
 
+    fp64_gops = wc.measure_fp64_rate(stream)
+
+    # the same workload in exact FP64 arithmetic (bit-identical to the
+    # reference), against both rooflines: HBM and the FP64 pipe
+    exact = None
+    if prec != 0:
+        st = max(20, args.steps // 5)
+        ms_x, _, _ = time_gpu(wc, bufs, n, filt, 0, J, 0, stream, st, 3)
+        gs = st * n / (ms_x / 1e3) / 1e9
+        ops = fp64_ops_per_sample(0, filt, J)
+        exact = {"workload": f"DWT {FILTERS[filt]} fwd+inv, n=2^{args.log2n}, J={J}, exact FP64",
+                 "steps": st, "gsamples_s": gs, "ms_per_step": ms_x / st,
+                 "hbm_frac": step_bytes(0, n, J, 8) * st / (ms_x / 1e3) / 1e9 / hbm,
+                 "fp64_ops_per_sample": ops, "fp64_gops": gs * ops,
+                 "fp64_peak_gops": fp64_gops, "fp64_frac": gs * ops / fp64_gops,
+                 "bound": "fp64 pipe (min of HBM and FP64 roofline)"}
+
     out = {"metric": METRIC, "value": value, "unit": "Gsamples/s", "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -353,7 +385,9 @@ def ours(args):
                       "l2": f"inputs ({n * esz >> 20} MiB) larger than L2; no flush",
                       "parallelism": f"replicas x{dist.world}"},
            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-           "pr_err": pr_err}
+           "pr_err": pr_err, "fp64_rate_gops": fp64_gops}
+    if exact:
+        out["exact_fp64"] = exact
 
     if dist.rank == 0 and not args.no_cpu:
         v, kind, reps, tt, threads = cpu_time_dwt(1 << args.cpu_log2n, filt,
@@ -379,17 +413,22 @@ def ours(args):
                     esize = 4 if p == 2 else 8
                     gs = args.sweep_steps * n / (ms_s / 1e3) / 1e9
                     frac = step_bytes(ttype, n, Jt, esize) * args.sweep_steps / (ms_s / 1e3) / 1e9 / hbm
-                    sweep.append({"transform": "DWT" if ttype == 0 else "MODWT",
-                                  "filter": FILTERS[f], "J": Jt, "precision": PREC[p],
-                                  "gsamples_s": round(gs, 3), "hbm_frac": round(frac, 4),
-                                  "ms_per_step": round(ms_s / args.sweep_steps, 3)})
+                    ent = {"transform": "DWT" if ttype == 0 else "MODWT",
+                           "filter": FILTERS[f], "J": Jt, "precision": PREC[p],
+                           "gsamples_s": round(gs, 3), "hbm_frac": round(frac, 4),
+                           "ms_per_step": round(ms_s / args.sweep_steps, 3)}
+                    if p == 0:
+                        ent["fp64_frac"] = round(gs * fp64_ops_per_sample(ttype, f, Jt)
+                                                 / fp64_gops, 4)
+                    sweep.append(ent)
                     if p == 2:
                         xf.free()
         out["sweep"] = sweep
     if tiling:
         out["tiling"] = tiling
     # Optional sections: a failure is recorded in the line, not fatal to it.
-    for key, skip, fn in (("batched", args.no_batch, batch_bench), ("tuned", args.no_fit, fit_bench),
+    for key, skip, fn in (("fp32_error", args.no_error, error_report),
+                          ("batched", args.no_batch, batch_bench), ("tuned", args.no_fit, fit_bench),
                           ("smooth", args.no_smooth, smooth_bench)):
         if skip:
             continue
@@ -401,31 +440,108 @@ def ours(args):
         print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------ error report --
+
+def _level_stats(got, ref, blocks):
+    rows = []
+    for name, sl in blocks:
+        d = got[sl] - ref[sl]
+        scale = float(np.max(np.abs(ref[sl]))) or 1.0
+        rows.append({"level": name, "max_abs": float(np.max(np.abs(d))),
+                     "rms": float(np.sqrt(np.mean(d * d))),
+                     "max_rel": float(np.max(np.abs(d))) / scale})
+    return rows
+
+
+def error_report(wc, args):
+    """Error of the FP32 path (and of the double-float FP64 path) against the
+    FP64 oracle, per filter and level: max |error|, RMS error and max |error|
+    over the level block's largest coefficient.  DWT J = 16 at n = 2^26 and
+    TO-MODWT J = 12 at n = 2^24 (the oracle's MODWT array at 2^26 would take
+    13 GB of host memory per copy); FP32 inputs are the FP64 signal rounded to
+    FP32, so the error includes that rounding.  Inverse: reconstruction of
+    the oracle's coefficients against the oracle's inverse."""
+    from wavecuda_gb300 import signals
+    impl, kind, threads = cpu_impl(use_ref=False)
+    L = wc.lib()
+    out = {"reference": f"oracle port ({kind}), FP64", "oracle_threads": threads}
+    for ttype, lg, J in ((0, args.error_log2n, 16), (1, args.error_log2n - 2, 12)):
+        n = 1 << lg
+        x = signals.roofline_input(n, seed=33)
+        tname = "DWT" if ttype == 0 else "MODWT"
+        for f in (1, 2, 3, 4):
+            if ttype == 0:
+                ref = impl.dwt(x, J, f)
+                blocks = [(f"d{lv}", slice(1 << (lv - 1), n, 1 << lv)) for lv in range(1, J + 1)]
+                blocks.append((f"s{J}", slice(0, n, 1 << J)))
+                rinv = impl.dwt(ref, J, f, 0)
+                nout = n
+            else:
+                ref = impl.modwt_fwd(x, J, f)
+                blocks = []
+                for lv in range(J):
+                    blocks.append((f"s{lv + 1}", slice(2 * lv * n, (2 * lv + 1) * n)))
+                    blocks.append((f"d{lv + 1}", slice((2 * lv + 1) * n, (2 * lv + 2) * n)))
+                rinv = impl.modwt_inv(ref, n, J, f)
+                nout = 2 * n * J
+            for p in (2, 1):
+                dt = np.float32 if p == 2 else np.float64
+                es = np.dtype(dt).itemsize
+                a, b = wc.DeviceBuffer(es * n), wc.DeviceBuffer(es * nout)
+                a.upload(x.astype(dt))
+                if ttype == 0:
+                    wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, J, f, p, None))
+                else:
+                    wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 1, J, f, p, None))
+                got = b.download(dt, nout).astype(np.float64)
+                fwd = _level_stats(got, ref, blocks)
+                del got
+                b.upload(ref.astype(dt))
+                if ttype == 0:
+                    wc.check(L.wc_dwt_device(b.ptr, a.ptr, n, 0, J, f, p, None))
+                else:
+                    wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 0, J, f, p, None))
+                r = a.download(dt, n).astype(np.float64)
+                a.free(); b.free()
+                d = r - rinv
+                out[f"{tname} {FILTERS[f]} J={J} n=2^{lg}/{PREC[p]}"] = {
+                    "forward": fwd,
+                    "forward_max_rel": max(e["max_rel"] for e in fwd),
+                    "inverse": {"max_abs": float(np.max(np.abs(d))),
+                                "rms": float(np.sqrt(np.mean(d * d))),
+                                "max_rel": float(np.max(np.abs(d)) / np.max(np.abs(rinv)))}}
+    return out
+
+
 # ------------------------------------------------------- batched smoothing --
 
 def make_batch(wc, nsig, seed):
-    """4096-signal workload: lengths 2^k, k uniform on 10..20; random filter,
-    random transform, J = min(k, 10) clamped to the level limit; universal or
-    CV soft thresholds; signals shaped like doppler/blocks/bumps/heavisine at
-    SNR 3 or 7."""
+    """4096-signal workload (signals.batch_workload): lengths 2^k, k uniform
+    on 10..20; random filter, random transform, J = min(k, 10) clamped to the
+    level limit; universal or CV soft thresholds; signals shaped like
+    doppler/blocks/bumps/heavisine at SNR 3 or 7."""
     from wavecuda_gb300 import signals as sg
-    rng = np.random.default_rng(seed)
-    shapes = list(sg.SHAPES)
-    sigs, chunks, clean, off = [], [], [], 0
-    for i in range(nsig):
-        k = int(rng.integers(10, 21))
-        n = 1 << k
-        filt = int(rng.integers(1, 5))
-        ttype = int(rng.integers(0, 2))
-        J = min(k, 10, wc.max_levels(n, filt))
-        tt = int(rng.choice([wc.UNIV, wc.CV]))
-        f = sg.SHAPES[shapes[int(rng.integers(0, 4))]](n, i)
-        x = sg.noisy(f, float(rng.choice([3.0, 7.0])), seed=seed * 7919 + i)
-        chunks.append(x)
-        clean.append(f)
-        sigs.append(wc.Signal(off, n, J, ttype, filt, tt, wc.SOFT, 0, J - 1, 0.0, 1e-8))
-        off += n
-    return np.concatenate(chunks), sigs, np.concatenate(clean)
+    data, specs, clean = sg.batch_workload(nsig, seed, wc.max_levels)
+    sigs = [wc.Signal(s["offset"], s["len"], s["nlevels"], s["ttype"], s["filter"],
+                      s["threshtype"], s["hardness"], s["minlevel"], s["maxlevel"], s["thresh"],
+                      s["tol"]) for s in specs]
+    return data, sigs, clean
+
+
+def smooth_bytes(ttype: int, n: int, J: int, threshtype: int, iterations: int,
+                 esize: int) -> float:
+    """Algorithmic HBM bytes of one smoothing: forward and inverse transform
+    of the full signal; for CV also the forward transforms of the two halves
+    (J - 1 levels) and, per golden-section step, two half-length inverse
+    transforms plus the loss pass (read both reconstructions and the signal,
+    2 * n/2 values in esize bytes and n FP64 values)."""
+    b = step_bytes(ttype, n, J, esize)
+    if threshtype == 2 and J > 1:
+        h = n // 2
+        fwd_h = (2 * h if ttype == 0 else (1 + 2 * (J - 1)) * h) * esize
+        inv_h = (2 * h if ttype == 0 else (J - 1 + 2) * h) * esize
+        b += 2 * fwd_h + iterations * (2 * inv_h + n * esize + 8 * n)
+    return float(b)
 
 
 def batch_bench(wc, args):
@@ -437,7 +553,8 @@ def batch_bench(wc, args):
            "samples": int(data.size)}
     rng = np.random.default_rng(5)
     sub = sorted(rng.choice(len(sigs), size=min(args.plain_signals, len(sigs)), replace=False))
-    for prec in (1, 2):
+    hbm, _ = peaks()
+    for prec in (0, 1, 2):
         r = {}
         arr = (wc.Signal * len(sigs))(*sigs)
         plan = C.c_void_p()
@@ -493,6 +610,12 @@ def batch_bench(wc, args):
         r["grid"] = grid.value
         r["mse_vs_clean"] = mse
         r["cv_iterations_mean"] = float(np.mean([x.iterations for x in res if x.iterations]))
+        es = 4 if prec == 2 else 8
+        tot = sum(smooth_bytes(s_.ttype, s_.len, s_.nlevels, s_.threshtype, res[i].iterations, es)
+                  for i, s_ in enumerate(sigs))
+        r["algorithmic_bytes"] = tot
+        r["aggregate_gbs"] = tot / (dev_ms / 1e3) / 1e9
+        r["hbm_frac"] = r["aggregate_gbs"] / hbm
         out[PREC[prec]] = r
     return out
 
@@ -647,7 +770,8 @@ def profile_case(args):
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
     es = 4 if prec == 2 else 8
-    a, b, r = wc.DeviceBuffer(es * n), wc.DeviceBuffer(es * n * 2 * 4), wc.DeviceBuffer(es * n)
+    nb = n if kind == "dwt" else n * 2 * 4
+    a, b, r = wc.DeviceBuffer(es * n), wc.DeviceBuffer(es * nb), wc.DeviceBuffer(es * n)
     a.upload(x.astype(np.float32) if prec == 2 else x)
     if args.tiling:
         wc.set_dwt_tiling(filt, prec, *[int(v) for v in args.tiling.split(":")])
@@ -684,8 +808,10 @@ def main():
     ap.add_argument("--fit-signals", type=int, default=256)
     ap.add_argument("--tiling", default=None,
                     help="tile:g0:threads:pipelined for --profile-case")
-    ap.add_argument("--sweep-steps", type=int, default=2)
+    ap.add_argument("--sweep-steps", type=int, default=20)
+    ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--error-log2n", type=int, default=26)
     ap.add_argument("--cpu-log2n", type=int, default=24)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--profile-case", default=None,

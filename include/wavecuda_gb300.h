@@ -66,7 +66,7 @@ extern "C" {
 #define WC_ERR_NOMEM 4       /* device or pinned host allocation failed */
 #define WC_ERR_UNSUPPORTED 5 /* combination not provided */
 #define WC_ERR_NODEVICE 6    /* no usable CUDA device */
-#define WC_ERR_TIMEOUT 7     /* a bounded device-side wait gave up */
+#define WC_ERR_TIMEOUT 7     /* a bounded device-side wait gave up; results incomplete */
 
 #define WC_F64_EXACT 0
 #define WC_F64_FAST 1
@@ -102,6 +102,41 @@ WC_API void RcpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filte
 WC_API void RgpuSmooth(double* x, int* len, int* nlevels, int* ttype, int* filter,
                 int* filterlen, int* threshtype, double* thresh, int* hardness,
                 int* minlevel, int* maxlevel, double* tol);
+
+/* ---- .C glue with a status (R's .C passes only pointers to vector
+ * elements; the wc_* calls below take scalars by value and structs).  Each
+ * writes WC_OK or an error code to *status and prints nothing.  No
+ * counterpart in the reference, whose symbols return no status
+ * (rfunctions.cu:3-137). */
+
+/* wc_transform through pointers: rfunctions.cu:21 (RgpuTransform) plus an
+ * explicit precision and a status. */
+WC_API void wc_transform_R(double* x, double* xmod, int* len, int* sense, int* nlevels,
+                           int* ttype, int* filter, int* precision, int* status);
+/* wc_threshold through pointers: rfunctions.cu:59 (RcpuThreshold) plus a
+ * status. */
+WC_API void wc_threshold_R(double* x, double* xmod, int* len, int* nlevels, int* ttype,
+                           int* filter, double* thresh, int* hardness, int* minlevel,
+                           int* maxlevel, int* status);
+/* wc_smooth through pointers: rfunctions.cu:102 (RgpuSmooth) plus an
+ * explicit precision and a status. */
+WC_API void wc_smooth_R(double* x, int* len, int* nlevels, int* ttype, int* filter,
+                        int* threshtype, double* thresh, int* hardness, int* minlevel,
+                        int* maxlevel, double* tol, int* precision, int* status);
+/* Batched smoothing in flat .C form -- the role of the reference's list API
+ * RgpuTransformList (rfunctions.cu:139-154, a .Call placeholder whose R
+ * wrapper is commented out at rfunctions.R:614-643).  Signal i occupies
+ * data[offset[i] .. offset[i] + len[i]) (0-based; *total values in all) and
+ * is described by element i of the parallel vectors (codes as for
+ * RgpuSmooth).  thresh[i]: manual threshold in, threshold applied out;
+ * iterations, kept, zeroed (may be NULL): CV iterations and kept/zeroed
+ * detail counts out.  One persistent launch smooths every signal
+ * (wc_smooth_batch). */
+WC_API void RgpuSmoothBatch(double* data, int* total, int* nsig, int* offset, int* len,
+                            int* nlevels, int* ttype, int* filter, int* threshtype,
+                            double* thresh, int* hardness, int* minlevel, int* maxlevel,
+                            double* tol, int* precision, int* iterations, int* kept,
+                            int* zeroed, int* status);
 
 /* ------------------------------------------------ 2. status-returning API */
 
@@ -215,8 +250,11 @@ WC_API int wc_dwt_device(const void* in, void* out, int64_t len, int sense,
  * the library, which every GPU that loads it holds until the process exits.
  * Limit: len <= 2^22 samples (longer lengths are rejected with WC_ERR_ARG).
  * The first call on a device looks up the array's device address for that
- * device; make it before any stream capture.  All calls share the array and
- * it keeps the last call's contents, so calls that overlap on the GPU race.
+ * device; make it before any stream capture (later calls look it up again
+ * unless their stream is capturing).  All calls share the array and it keeps
+ * the last call's contents, so calls that overlap on the GPU race.  Its
+ * status word is sticky: a bounded wait that gave up sets bit 0, and
+ * wc_device_status() (which allocates nothing) reads and clears it.
  * stream NULL means the legacy default stream (other wc_* calls given NULL
  * use the library's non-blocking stream, which is not ordered with it, so
  * pass the same explicit stream when mixing them).  Calls no cudaMalloc or
@@ -410,10 +448,38 @@ typedef struct {
 WC_API int wc_profile_start(void);
 WC_API int wc_profile_stop(wc_kernel_time* out, int capacity, int* count);
 
-/* Reads and clears the current device's status word after synchronising:
- * bit 0 set means a bounded device-side wait (bulk-copy barrier) gave up and
- * the kernel that waited skipped its work.  0 when all is well. */
+/* Reads and clears the current device's status words after synchronising
+ * the device: the workspace word of the device-pointer calls and the word of
+ * wc_dwt_device_noalloc.  Bit 0 set means a bounded device-side wait
+ * (bulk-copy barrier) gave up and the kernel that waited skipped its work.
+ * 0 when all is well.  Allocates nothing.  (The host-buffer calls and the
+ * reference symbols read the workspace word themselves after their work: they
+ * return WC_ERR_TIMEOUT -- the reference symbols print it -- and leave the
+ * caller's buffers untouched, except a long DWT streamed in place over the
+ * host link, which has already written part of x.) */
 WC_API int wc_device_status(unsigned int* status);
+
+/* ---- test hooks.  Failure injection without a GPU fault: the library's
+ * allocation failures and its bounded waits can be made to happen on
+ * purpose, so that their error paths can be tested. */
+/* Every workspace slot that would have to grow beyond `bytes` fails with
+ * WC_ERR_NOMEM instead of calling cudaMalloc (0 removes the cap). */
+WC_API int wc_debug_set_workspace_cap(size_t bytes);
+/* Bytes of device workspace the library holds on the current device. */
+WC_API int wc_debug_workspace_bytes(size_t* bytes);
+/* Launches one small kernel that arms an mbarrier for 16 bytes which no copy
+ * delivers, so the library's bounded wait gives up after `polls` polls
+ * (1..2^20) and records a timeout in a status word: target 0 the workspace
+ * word, 1 the word of wc_dwt_device_noalloc.  Asynchronous; read the result
+ * with wc_device_status() or through the next host-buffer call. */
+WC_API int wc_debug_wait_probe(int target, unsigned int polls, void* stream);
+
+/* Measured FP64 add/multiply throughput of the current device, in billions
+ * of separately rounded FP64 operations per second (a short kernel of
+ * independent multiply-add chains, never contracted to FMA, timed with CUDA
+ * events): the arithmetic roofline of the WC_F64_EXACT kernels, which issue
+ * exactly such operations.  Synchronous. */
+WC_API int wc_measure_fp64_rate(double* gops, void* stream);
 
 /* Number of kernels this library launched in this process so far. */
 WC_API int64_t wc_kernel_launch_count(void);

@@ -8,9 +8,17 @@ takes signals up to 2^22 samples.  Here it is called through the C ABI and
 checked against the regular entry point (wc_dwt_device), twice in a row, with
 the tolerances the other transform tests use (bit-identical in exact FP64).
 This file is collected last so that a failure here comes after every other
-test has run; it also passes on its own in a fresh process.
+test has run; it also passes on its own in a fresh process.  The last tests
+check the two promises that the regular entry point cannot show: a fresh
+process that calls only this entry point ends with no library workspace on
+the device, and a timed-out wait in its kernels is reported through its own
+status word (read by wc_device_status, which allocates nothing either).
 """
 import ctypes as C
+import os
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -71,3 +79,41 @@ def test_noalloc_rejects_lengths_beyond_its_maximum(gpu):
     r = noalloc(a.ptr, b.ptr, n, 1, 0, 2, 0, gpu.default_stream())
     assert r == 1 and "maximum" in gpu.last_error()
     a.free(); b.free()
+
+
+def test_noalloc_timeout_reaches_its_own_status_word(gpu):
+    # The probe's barrier expects bytes that never arrive; its bounded wait
+    # gives up and sets bit 0 of the allocation-free DWT's status word.
+    assert gpu.device_status() == 0
+    gpu.debug_wait_probe(target=1, polls=1000)
+    assert gpu.device_status() == 1
+    assert gpu.device_status() == 0
+
+
+def test_noalloc_fresh_process_holds_no_workspace():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = textwrap.dedent("""
+        import ctypes as C, sys
+        import numpy as np
+        sys.path.insert(0, %r)
+        import wavecuda_gb300 as wc
+        lib = wc.lib()
+        f = lib.wc_dwt_device_noalloc
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_int64] + [C.c_int] * 4 + [C.c_void_p]
+        n = 1 << 20
+        x = np.random.default_rng(0).standard_normal(n)
+        a, b, c = wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n), wc.DeviceBuffer(8 * n)
+        s = wc.default_stream()  # one stream for the copies and the calls
+        a.upload(x, s)
+        for _ in range(2):
+            wc.check(f(a.ptr, b.ptr, n, 1, 0, 4, 0, s))
+            wc.check(f(b.ptr, c.ptr, n, 0, 0, 4, 0, s))
+        r = c.download(np.float64, n, s)
+        assert np.max(np.abs(r - x)) < 1e-12 * np.max(np.abs(x))
+        assert wc.device_status() == 0
+        assert wc.debug_workspace_bytes() == 0, wc.debug_workspace_bytes()
+        print("noalloc-fresh-ok")
+    """ % root)
+    out = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0 and "noalloc-fresh-ok" in out.stdout, out.stdout + out.stderr

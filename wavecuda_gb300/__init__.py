@@ -164,6 +164,20 @@ def lib() -> C.CDLL:
                                       _vp, _vp]
     L.wc_wst_table.argtypes = [_dp, C.c_int64, C.c_int, C.c_int, C.c_int, _dp,
                                C.POINTER(C.c_int32), _dp, C.POINTER(C.c_uint8)]
+    for name in ("wc_transform_R",):
+        getattr(L, name).argtypes = [_dp, _dp] + [_ip] * 7
+        getattr(L, name).restype = None
+    L.wc_threshold_R.argtypes = [_dp, _dp] + [_ip] * 4 + [_dp, _ip, _ip, _ip, _ip]
+    L.wc_threshold_R.restype = None
+    L.wc_smooth_R.argtypes = [_dp] + [_ip] * 5 + [_dp, _ip, _ip, _ip, _dp, _ip, _ip]
+    L.wc_smooth_R.restype = None
+    L.RgpuSmoothBatch.argtypes = ([_dp, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _ip, _ip,
+                                   _ip, _dp, _ip, _ip, _ip, _ip, _ip])
+    L.RgpuSmoothBatch.restype = None
+    L.wc_measure_fp64_rate.argtypes = [_dp, _vp]
+    L.wc_debug_set_workspace_cap.argtypes = [C.c_size_t]
+    L.wc_debug_workspace_bytes.argtypes = [C.POINTER(C.c_size_t)]
+    L.wc_debug_wait_probe.argtypes = [C.c_int, C.c_uint, _vp]
     _lib = L
     return L
 
@@ -616,9 +630,63 @@ def smooth_batch(data, signals, precision=F64_EXACT):
     return y, list(res)
 
 
+def smooth_batch_R(data, signals, precision=F64_EXACT):
+    """The flat .C form RgpuSmoothBatch, called exactly as R's .C would:
+    every argument a pointer to a double or int vector.  Returns (smoothed
+    copy, thresholds, iterations, kept, zeroed, status)."""
+    y = np.array(data, dtype=np.float64, copy=True)
+    k = len(signals)
+
+    def iv(field):
+        return np.ascontiguousarray([getattr(s_, field) for s_ in signals], dtype=np.int32)
+
+    vecs = {f: iv(f) for f in ("offset", "len", "nlevels", "ttype", "filter", "threshtype",
+                               "hardness", "minlevel", "maxlevel")}
+    th = np.ascontiguousarray([s_.thresh for s_ in signals], dtype=np.float64)
+    tol = np.ascontiguousarray([s_.tol for s_ in signals], dtype=np.float64)
+    its, kept, zer = (np.zeros(k, dtype=np.int32) for _ in range(3))
+    total, nsig, prec, status = (np.array([v], dtype=np.int32)
+                                 for v in (y.size, k, precision, -1))
+
+    def ip(a):
+        return a.ctypes.data_as(_ip)
+
+    lib().RgpuSmoothBatch(_dptr(y), ip(total), ip(nsig), ip(vecs["offset"]), ip(vecs["len"]),
+                          ip(vecs["nlevels"]), ip(vecs["ttype"]), ip(vecs["filter"]),
+                          ip(vecs["threshtype"]), _dptr(th), ip(vecs["hardness"]),
+                          ip(vecs["minlevel"]), ip(vecs["maxlevel"]), _dptr(tol), ip(prec),
+                          ip(its), ip(kept), ip(zer), ip(status))
+    return y, th, its, kept, zer, int(status[0])
+
+
 def device_status() -> int:
+    """Reads and clears the status words (bit 0: a bounded wait gave up)."""
     v = C.c_uint(0)
     check(lib().wc_device_status(C.byref(v)))
+    return v.value
+
+
+def measure_fp64_rate(stream=None) -> float:
+    """Measured FP64 add/multiply rate of the device (G operations/s)."""
+    v = C.c_double(0.0)
+    check(lib().wc_measure_fp64_rate(C.byref(v), stream))
+    return v.value
+
+
+def debug_wait_probe(target=0, polls=1000, stream=None) -> None:
+    """Test hook: makes one bounded device-side wait run out (see
+    wc_debug_wait_probe)."""
+    check(lib().wc_debug_wait_probe(target, polls, stream))
+
+
+def debug_set_workspace_cap(nbytes: int) -> None:
+    """Test hook: workspace growth beyond nbytes fails with WC_ERR_NOMEM."""
+    check(lib().wc_debug_set_workspace_cap(nbytes))
+
+
+def debug_workspace_bytes() -> int:
+    v = C.c_size_t(0)
+    check(lib().wc_debug_workspace_bytes(C.byref(v)))
     return v.value
 
 

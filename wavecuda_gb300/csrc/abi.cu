@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "wc_bulk.cuh"
 #include "wc_common.cuh"
 
 namespace wc {
@@ -103,6 +104,9 @@ struct DeviceState {
 std::mutex g_mu;
 std::map<int, DeviceState> g_dev;
 thread_local int g_ws_err = WC_OK;
+// Largest workspace slot the library may grow to (0: no cap).  A test hook
+// (wc_debug_set_workspace_cap) that makes allocation failure reproducible.
+std::atomic<size_t> g_ws_cap{0};
 
 DeviceState& state() {
   int d = 0;
@@ -117,6 +121,12 @@ void* workspace(Slot slot, size_t bytes) {
   DeviceState& st = state();
   if (bytes == 0) bytes = 256;
   if (st.size[slot] >= bytes) return st.slot[slot];
+  const size_t cap = g_ws_cap.load();
+  if (cap != 0 && bytes > cap) {
+    g_ws_err = fail(WC_ERR_NOMEM, "device allocation of %zu bytes refused (workspace cap %zu)",
+                    bytes, cap);
+    return nullptr;
+  }
   if (st.slot[slot]) {
     // Work queued on other streams may still use the old buffer.
     cudaDeviceSynchronize();
@@ -156,6 +166,20 @@ unsigned int* device_status_word() {
 
 int workspace_error() { return g_ws_err == WC_OK ? WC_ERR_NOMEM : g_ws_err; }
 
+int take_status(cudaStream_t s) {
+  unsigned int* w = device_status_word();
+  if (!w) return workspace_error();
+  unsigned int h = 0;
+  WC_CUDA(cudaMemcpyAsync(&h, w, sizeof(h), cudaMemcpyDeviceToHost, s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  if (h == 0) return WC_OK;
+  WC_CUDA(cudaMemsetAsync(w, 0, sizeof(unsigned int), s));
+  WC_CUDA(cudaStreamSynchronize(s));
+  return fail(WC_ERR_TIMEOUT,
+              "a bounded device-side wait gave up (status 0x%x): the results of this call, or "
+              "of an earlier asynchronous call on this device, are incomplete", h);
+}
+
 int ensure_device() {
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
@@ -181,6 +205,49 @@ int check_levels(int64_t n, int nlevels, int filterlen) {
   if (nlevels == 0) nlevels = maxlevels;
   if (nlevels < 0 || nlevels > maxlevels) return 0;
   return nlevels;
+}
+
+unsigned int* existing_status_word() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  auto it = g_dev.find(d);
+  return it == g_dev.end() ? nullptr : static_cast<unsigned int*>(it->second.slot[kSlotStatus]);
+}
+
+// FP64 pipe rate: eight independent chains x <- fl(fl(x * a) + b) per
+// thread, every operation a separately rounded __dmul_rn / __dadd_rn as the
+// exact-mode kernels issue them (never contracted to an FMA).
+__global__ void __launch_bounds__(256) fp64_rate_kernel(double* out, int iters, double a,
+                                                        double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = __dadd_rn(__dmul_rn(x[k], a), b);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) t += x[k];
+  if (t == -1.0) out[0] = t;  // never true; keeps the chains alive
+}
+
+// Test of the bounded waits: thread 0 arms an mbarrier for 16 bytes that no
+// copy ever delivers, so its phase never completes; mbar_wait gives up after
+// `polls` polls, records the timeout in *status and the kernel returns.  No
+// asynchronous copy is issued, so nothing is in flight when it exits.
+__global__ void wait_probe_kernel(unsigned int* status, unsigned int polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, 16);
+    mbar_wait(&bar, 0, status, polls);
+    mbar_inval(&bar);
+  }
 }
 
 }  // namespace wc
@@ -292,8 +359,9 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
     const int r = dwt_host_inplace(x, len, sense, J, filter, prec, s);
     if (r != WC_ERR_UNSUPPORTED) {
       WC_TRY(r);
-      WC_CUDA(cudaStreamSynchronize(s));
-      return WC_OK;
+      // The streamed path writes x in place as it goes: a timeout is
+      // reported, but x already holds partial results.
+      return take_status(s);
     }
   }
   if (ttype == 0) {
@@ -305,6 +373,7 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
     } else {
       WC_TRY(dwt(A, B, len, sense, J, filter, prec, s));
     }
+    WC_TRY(take_status(s));  // x stays untouched when a wait gave up
     WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
   } else {
     // time order (ttype 1) or packet order (ttype 2, modwt_po)
@@ -321,6 +390,7 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
       } else {
         WC_TRY(mod(B, A, 1));
       }
+      WC_TRY(take_status(s));
       WC_CUDA(cudaMemcpyAsync(xmod, A, bm, cudaMemcpyDeviceToHost, s));
     } else {
       WC_CUDA(cudaMemcpyAsync(A, xmod, bm, cudaMemcpyHostToDevice, s));
@@ -331,6 +401,7 @@ int transform_host(double* x, double* xmod, int64_t len, int sense, int nlevels,
       } else {
         WC_TRY(mod(B, A, 0));
       }
+      WC_TRY(take_status(s));
       WC_CUDA(cudaMemcpyAsync(x, B, bx, cudaMemcpyDeviceToHost, s));
     }
   }
@@ -367,6 +438,7 @@ int threshold_host(double* x, double* xmod, int64_t len, int nlevels, int ttype,
   } else {
     WC_TRY(wc::threshold(A, len, J, ttype, t, hardness, minl, maxl, WC_F64_EXACT, s));
   }
+  WC_TRY(take_status(s));
   WC_CUDA(cudaMemcpyAsync(data, A, b, cudaMemcpyDeviceToHost, s));
   WC_CUDA(cudaStreamSynchronize(s));
   return WC_OK;
@@ -390,8 +462,11 @@ int smooth_host(double* x, int64_t len, int nlevels, int ttype, int filter, int 
   double* A = static_cast<double*>(workspace(kSlotStageA, b));
   if (!A) return workspace_error();
   WC_CUDA(cudaMemcpyAsync(A, x, b, cudaMemcpyHostToDevice, s));
-  WC_TRY(wc::smooth(A, len, J, ttype, filter, threshtype, thresh, hardness, minl, maxl, tol, prec,
+  double t = *thresh;
+  WC_TRY(wc::smooth(A, len, J, ttype, filter, threshtype, &t, hardness, minl, maxl, tol, prec,
                     s, info));
+  WC_TRY(take_status(s));  // x and *thresh stay untouched when a wait gave up
+  *thresh = t;
   WC_CUDA(cudaMemcpyAsync(x, A, b, cudaMemcpyDeviceToHost, s));
   WC_CUDA(cudaStreamSynchronize(s));
   return WC_OK;
@@ -597,14 +672,94 @@ int64_t wc_kernel_launch_count(void) { return g_launches.load(); }
 int wc_device_status(unsigned int* status) {
   clear_error();
   WC_TRY(ensure_device());
-  unsigned int* w = device_status_word();
-  if (!w) return workspace_error();
+  if (!status) return fail(WC_ERR_ARG, "null status pointer");
   WC_CUDA(cudaDeviceSynchronize());
   unsigned int h = 0;
-  WC_CUDA(cudaMemcpy(&h, w, sizeof(h), cudaMemcpyDeviceToHost));
-  WC_CUDA(cudaMemset(w, 0, sizeof(unsigned int)));
+  // The workspace word exists once a kernel that waits has been launched,
+  // the allocation-free DWT's word once that entry point has run on this
+  // device; neither is created here, so this call allocates nothing.
+  unsigned int* words[2] = {existing_status_word(), noalloc_status_word_if_known()};
+  for (unsigned int* w : words) {
+    if (!w) continue;
+    unsigned int v = 0;
+    WC_CUDA(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
+    if (v) WC_CUDA(cudaMemset(w, 0, sizeof(unsigned int)));
+    h |= v;
+  }
   *status = h;
   return WC_OK;
+}
+
+int wc_measure_fp64_rate(double* gops, void* stream) {
+  clear_error();
+  WC_TRY(ensure_device());
+  if (!gops) return fail(WC_ERR_ARG, "null pointer");
+  cudaStream_t s = pick(stream);
+  int dev = 0, sms = 1;
+  WC_CUDA(cudaGetDevice(&dev));
+  WC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  double* sink = static_cast<double*>(workspace(kSlotReduce, 256));
+  if (!sink) return workspace_error();
+  cudaEvent_t e0, e1;
+  WC_CUDA(cudaEventCreate(&e0));
+  WC_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int rc = WC_OK;
+  for (int rep = 0; rep < 4 && rc == WC_OK; rep++) {
+    cudaEventRecord(e0, s);
+    fp64_rate_kernel<<<blocks, threads, 0, s>>>(sink, iters, 0.9999999, 1e-7);
+    rc = after_launch("fp64_rate_kernel");
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(WC_ERR_CUDA, "fp64 rate kernel failed");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;  // the first launch warms up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != WC_OK) return rc;
+  const double ops = (double)blocks * threads * iters * 8 * 2;
+  *gops = ops / (best * 1e-3) / 1e9;
+  return WC_OK;
+}
+
+// ---- test hooks (failure injection on the host side and bounded waits) ----
+
+int wc_debug_set_workspace_cap(size_t bytes) {
+  g_ws_cap = bytes;
+  return WC_OK;
+}
+
+int wc_debug_workspace_bytes(size_t* bytes) {
+  clear_error();
+  if (!bytes) return fail(WC_ERR_ARG, "null pointer");
+  std::lock_guard<std::mutex> lk(g_mu);
+  int d = 0;
+  WC_CUDA(cudaGetDevice(&d));
+  size_t t = 0;
+  auto it = g_dev.find(d);
+  if (it != g_dev.end())
+    for (int i = 0; i < kNumSlots; i++) t += it->second.size[i];
+  *bytes = t;
+  return WC_OK;
+}
+
+int wc_debug_wait_probe(int target, unsigned int polls, void* stream) {
+  clear_error();
+  WC_TRY(ensure_device());
+  if (polls < 1 || polls > (1u << 20)) return fail(WC_ERR_ARG, "polls must lie in [1, 2^20]");
+  unsigned int* w = nullptr;
+  if (target == 0) {
+    w = device_status_word();
+    if (!w) return workspace_error();
+  } else if (target == 1) {
+    WC_TRY(noalloc_status_word(&w));
+  } else {
+    return fail(WC_ERR_ARG, "target must be 0 (workspace status word) or 1 (allocation-free DWT)");
+  }
+  wait_probe_kernel<<<1, 32, 0, pick(stream)>>>(w, polls);
+  return after_launch("wait_probe_kernel");
 }
 
 int wc_profile_start(void) {

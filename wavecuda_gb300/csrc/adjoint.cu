@@ -428,7 +428,7 @@ int sure_loss_grad(const double* y, int64_t n, int J, int F, int ttype, const do
   WC_TRY(after_launch("sure_div_kernel"));
   double h[kAccLen];
   WC_CUDA(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
-  WC_CUDA(cudaStreamSynchronize(s));
+  WC_TRY(take_status(s));
   // SURE = ||fh - y||^2 - n sigma^2 + 2 sigma^2 div, div = n - sum over
   // thresholded levels of kappa_l (count_l - smoothed kept_l).
   const double s2 = sigma * sigma;
@@ -483,7 +483,7 @@ int cv_loss_grad(const double* x, int64_t n, int J, int F, int ttype, const doub
   WC_TRY(soft_adjoint(co, ch, nullptr, acc + kAccGrad, h, Jh, ttype, lam, minl, maxh, s));
   double hv[kAccLen];
   WC_CUDA(cudaMemcpyAsync(hv, acc, sizeof(hv), cudaMemcpyDeviceToHost, s));
-  WC_CUDA(cudaStreamSynchronize(s));
+  WC_TRY(take_status(s));
   *loss = hv[kAccLoss];
   for (int l = 0; l < J; l++) grad[l] = (l < Jh && l >= minl && l <= maxh) ? hv[kAccGrad + l] : 0.0;
   return WC_OK;

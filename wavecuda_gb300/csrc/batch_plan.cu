@@ -312,6 +312,7 @@ int wc_smooth_batch(double* data, int64_t total, const wc_signal* sigs, int nsig
                                      cudaMemcpyHostToDevice, s) != cudaSuccess)
     rc = fail(WC_ERR_CUDA, "copy to device failed");
   if (rc == WC_OK) rc = wc_batch_run_device(plan, d, s);
+  if (rc == WC_OK) rc = take_status(s);  // data stay untouched when a wait gave up
   if (rc == WC_OK && cudaMemcpyAsync(data, d, sizeof(double) * (size_t)total,
                                      cudaMemcpyDeviceToHost, s) != cudaSuccess)
     rc = fail(WC_ERR_CUDA, "copy to host failed");

@@ -166,6 +166,7 @@ int wc_wst_table(const double* w, int64_t len, int nlevels, int ttype, int scali
   WC_CUDA(cudaMemcpyAsync(dw, w, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice, s));
   WC_TRY(launch_table(dw, len, nlevels, ttype, sc, W ? dW : nullptr, level ? dL : nullptr,
                       translate ? dT : nullptr, type ? dY : nullptr, s));
+  WC_TRY(take_status(s));
   if (W) WC_CUDA(cudaMemcpyAsync(W, dW, sizeof(double) * (size_t)rows, cudaMemcpyDeviceToHost, s));
   if (translate)
     WC_CUDA(cudaMemcpyAsync(translate, dT, sizeof(double) * (size_t)rows, cudaMemcpyDeviceToHost, s));

@@ -27,6 +27,7 @@
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
 #include "wc_taps2.cuh"
+#include "wc_dwt_math.cuh"
 
 namespace wc {
 namespace {
@@ -44,156 +45,6 @@ __host__ __device__ constexpr int64_t pad16(int64_t n) {
 // Right halo of the forward pass at level l of G (in level-l values).
 __host__ __device__ constexpr int64_t fwd_halo(int L, int G, int l) {
   return (int64_t)(L - 2) * (((int64_t)1 << (G - l)) - 1);
-}
-
-// Two adjacent values p[0], p[1] with one vector shared-memory access (p is
-// aligned to two values: every pair below starts at an even index of a
-// 16-byte-aligned buffer).
-template <class V>
-__device__ __forceinline__ void ld2(const V* p, V& a, V& b) {
-  if constexpr (std::is_same<V, dd>::value) {
-    const float4 t = *reinterpret_cast<const float4*>(p);
-    a = dd{t.x, t.y};
-    b = dd{t.z, t.w};
-  } else if constexpr (std::is_same<V, float>::value) {
-    const float2 t = *reinterpret_cast<const float2*>(p);
-    a = t.x;
-    b = t.y;
-  } else {
-    const double2 t = *reinterpret_cast<const double2*>(p);
-    a = t.x;
-    b = t.y;
-  }
-}
-
-template <class V>
-__device__ __forceinline__ void st2(V* p, V a, V b) {
-  if constexpr (std::is_same<V, dd>::value) {
-    *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
-  } else if constexpr (std::is_same<V, float>::value) {
-    *reinterpret_cast<float2*>(p) = make_float2(a, b);
-  } else {
-    *reinterpret_cast<double2*>(p) = make_double2(a, b);
-  }
-}
-
-// Tap pairs of the packed double-float dot products (empty for the other
-// policies), loaded once at the start of a kernel from constant memory
-// (wc_taps2.cuh): forward (h_j, g_j); inverse (h_2j, h_2j+1) and
-// (g_2j, g_2j+1).
-struct DwtTapTable {
-  TapPairF f[8], ih[4], ig[4];
-};
-constexpr DwtTapTable dwt_tap_table(int F) {
-  DwtTapTable t{};
-  for (int j = 0; j < filter_len(F); j++) t.f[j] = tap_pair_f(tap_h(F, j), tap_g(F, j));
-  for (int j = 0; j < filter_len(F) / 2; j++) {
-    t.ih[j] = tap_pair_f(tap_h(F, 2 * j), tap_h(F, 2 * j + 1));
-    t.ig[j] = tap_pair_f(tap_g(F, 2 * j), tap_g(F, 2 * j + 1));
-  }
-  return t;
-}
-__constant__ DwtTapTable kDwtTaps[5] = {DwtTapTable{}, dwt_tap_table(1), dwt_tap_table(2),
-                                        dwt_tap_table(3), dwt_tap_table(4)};
-
-template <int F, class P>
-struct PairTaps {
-  __device__ __forceinline__ void init() {}
-};
-template <int F>
-struct PairTaps<F, PDD> {
-  static constexpr int L = filter_len(F);
-  tap2 f[L], ih[L / 2], ig[L / 2];
-  __device__ __forceinline__ void init() {
-#pragma unroll
-    for (int j = 0; j < L; j++) f[j] = load_tap2(kDwtTaps[F].f[j]);
-#pragma unroll
-    for (int j = 0; j < L / 2; j++) {
-      ih[j] = load_tap2(kDwtTaps[F].ih[j]);
-      ig[j] = load_tap2(kDwtTaps[F].ig[j]);
-    }
-  }
-};
-
-template <int F, class P>
-__device__ __forceinline__ void fwd_pair(const typename P::V* src, typename P::V& s,
-                                         typename P::V& d, const PairTaps<F, P>& tp) {
-  using V = typename P::V;
-  constexpr int L = filter_len(F);
-  V v[L];
-#pragma unroll
-  for (int j = 0; j < L; j += 2) ld2(src + j, v[j], v[j + 1]);
-  if constexpr (F == 1) {
-    s = haar_sum<P>(v[0], v[1]);
-    d = haar_dif<P>(v[0], v[1]);
-  } else if constexpr (std::is_same<P, PDD>::value) {
-    // s in lane 0, d in lane 1: the same operations as below, packed.
-    // By extraction (wc_dd.cuh); sigma from sum_j |v_j| max(|h_j|, |g_j|).
-    float as = 0.f;
-#pragma unroll
-    for (int j = 0; j < L; j++) as = __fmaf_rn(fabsf(v[j].hi), tap_hg_max(F, j), as);
-    const f32x2 sig = extract_sigma(as);
-    dd_accx A = accx_init(v[0], tp.f[0], sig);
-#pragma unroll
-    for (int j = 1; j < L; j++) A = accx_add(A, v[j], tp.f[j], sig);
-    accx_fin(A, s, d);
-  } else {
-    typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
-    typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
-#pragma unroll
-    for (int j = 1; j < L; j++) {
-      as = P::acc_add(as, v[j], tap_h(F, j));
-      ad = P::acc_add(ad, v[j], tap_g(F, j));
-    }
-    s = P::acc_fin(as);
-    d = P::acc_fin(ad);
-  }
-}
-
-// Inverse step of one pair: even and odd outputs from s[-j] and d[-j]
-// (sv/dv in ascending j), taps in descending j as daub4.cpp:58-88.
-template <int F, class P>
-__device__ __forceinline__ void inv_pair(const typename P::V* sv, const typename P::V* dv,
-                                         typename P::V& e, typename P::V& o,
-                                         const PairTaps<F, P>& tp) {
-  constexpr int HH = filter_len(F) / 2;
-  if constexpr (F == 1) {
-    e = haar_sum<P>(sv[0], dv[0]);
-    o = haar_dif<P>(sv[0], dv[0]);
-  } else if constexpr (std::is_same<P, PDD>::value) {
-    // e in lane 0, o in lane 1: the same operations as below, packed.
-    // By extraction (wc_dd.cuh); sigma from the inputs' |.| times the
-    // larger of the two lanes' taps.
-    float as = 0.f;
-#pragma unroll
-    for (int j = 0; j < HH; j++) {
-      as = __fmaf_rn(fabsf(sv[j].hi), tap_pair_max(tap_h(F, 2 * j), tap_h(F, 2 * j + 1)), as);
-      as = __fmaf_rn(fabsf(dv[j].hi), tap_pair_max(tap_g(F, 2 * j), tap_g(F, 2 * j + 1)), as);
-    }
-    const f32x2 sig = extract_sigma(as);
-    dd_accx A = accx_init(sv[HH - 1], tp.ih[HH - 1], sig);
-    A = accx_add(A, dv[HH - 1], tp.ig[HH - 1], sig);
-#pragma unroll
-    for (int j = HH - 2; j >= 0; j--) {
-      A = accx_add(A, sv[j], tp.ih[j], sig);
-      A = accx_add(A, dv[j], tp.ig[j], sig);
-    }
-    accx_fin(A, e, o);
-  } else {
-    typename P::Acc ae = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1)));
-    typename P::Acc ao = P::acc_init(sv[HH - 1], tap_h(F, 2 * (HH - 1) + 1));
-    ae = P::acc_add(ae, dv[HH - 1], tap_g(F, 2 * (HH - 1)));
-    ao = P::acc_add(ao, dv[HH - 1], tap_g(F, 2 * (HH - 1) + 1));
-#pragma unroll
-    for (int j = HH - 2; j >= 0; j--) {
-      ae = P::acc_add(ae, sv[j], tap_h(F, 2 * j));
-      ao = P::acc_add(ao, sv[j], tap_h(F, 2 * j + 1));
-      ae = P::acc_add(ae, dv[j], tap_g(F, 2 * j));
-      ao = P::acc_add(ao, dv[j], tap_g(F, 2 * j + 1));
-    }
-    e = P::acc_fin(ae);
-    o = P::acc_fin(ao);
-  }
 }
 
 // Forward pass.  y[m] = in[m] (m < N, compact).  Writes the tile's
@@ -1191,15 +1042,19 @@ int dwt_host_inplace(double* x, int64_t n, int sense, int J, int F, int prec, cu
 // cudaMalloc from here would fail, or fragment that pool), or a latency-
 // critical loop that must not hit the device-wide synchronisation cudaFree
 // performs when the workspace grows.  For them the DWT's only scratch -- the
-// compact coarse coefficients handed from one pass to the next -- and the
-// device status word live in one file-scope device array of fixed size,
-// loaded with the library and held by every GPU that loads it until the
-// process exits.  Host code must not use the array's name as a device
-// address (it is a host-side stand-in); the device address comes from
-// cudaGetSymbolAddress, looked up once per device by the first call made
-// with that device current.  Make that first call before any stream capture.
+// compact coarse coefficients handed from one pass to the next -- and its
+// status word live in one file-scope device array of fixed size, loaded with
+// the library and held by every GPU that loads it until the process exits.
+// Host code must not use the array's name as a device address (it is a
+// host-side stand-in); the device address comes from cudaGetSymbolAddress,
+// looked up with the device current.  The first call on a device does that
+// set-up, so make it before any stream capture; later calls look the address
+// up again (which follows a reload of the module after a device reset) except
+// while their stream is capturing, when they use the address found before.
 // All calls share the array and it keeps the last call's contents: calls
 // whose work overlaps on the GPU (different streams, or threads) race on it.
+// The status word is sticky: a timed-out wait sets its bit, and only
+// wc_device_status() reads and clears it (the array starts zeroed).
 #include <mutex>
 
 namespace wc {
@@ -1215,21 +1070,31 @@ static __device__ __align__(256) unsigned char
 std::mutex g_noalloc_mu;
 void* g_noalloc_base[256] = {};
 
-// Device address of g_noalloc_scratch on the current device.
-int noalloc_base(unsigned char** base) {
+// Device address of g_noalloc_scratch on the current device.  Looked up
+// afresh unless the caller's stream is capturing (then the address found by
+// an earlier call is used; there must be one).
+int noalloc_base(unsigned char** base, cudaStream_t s, bool lookup) {
   int dev = 0;
   WC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 256) return fail(WC_ERR_ARG, "device ordinal %d out of range", dev);
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_base[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      cudaGetLastError();
-      return fail(WC_ERR_CUDA, "cudaGetSymbolAddress of the static DWT scratch failed: %s",
-                  cudaGetErrorString(e));
+  if (lookup) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    WC_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone || !g_noalloc_base[dev]) {
+      if (cs != cudaStreamCaptureStatusNone)
+        return fail(WC_ERR_ARG,
+                    "allocation-free DWT: the first call on a device must come before stream "
+                    "capture (it looks up the static scratch's device address)");
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(WC_ERR_CUDA, "cudaGetSymbolAddress of the static DWT scratch failed: %s",
+                    cudaGetErrorString(e));
+      }
+      g_noalloc_base[dev] = p;
     }
-    g_noalloc_base[dev] = p;
   }
   *base = static_cast<unsigned char*>(g_noalloc_base[dev]);
   return WC_OK;
@@ -1251,8 +1116,8 @@ int run_dwt_noalloc(const void* vin, void* vout, int64_t n, int sense, int J, cu
   if (np > 1 && sizeof(T) * (size_t)(plan[0].N >> plan[0].G) > kNoAllocCoarseBytes)
     return fail(WC_ERR_ARG, "allocation-free DWT: coarse scratch of %zu bytes exceeds %zu",
                 sizeof(T) * (size_t)(plan[0].N >> plan[0].G), kNoAllocCoarseBytes);
-  // The status word must start at zero for this call.
-  WC_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned int), s));
+  // The status word is not cleared here: a timeout of an earlier call stays
+  // visible until wc_device_status() reads it.
   if (sense == 1) {
     const T* src = in;
     for (int p = 0; p < np; p++) {
@@ -1309,6 +1174,20 @@ int dispatch_noalloc(const void* in, void* out, int64_t n, int sense, int J, int
 }
 
 }  // namespace
+
+unsigned int* noalloc_status_word_if_known() {
+  unsigned char* b = nullptr;
+  if (noalloc_base(&b, nullptr, false) != WC_OK) return nullptr;
+  return reinterpret_cast<unsigned int*>(b);
+}
+
+int noalloc_status_word(unsigned int** w) {
+  unsigned char* b = nullptr;
+  WC_TRY(noalloc_base(&b, nullptr, true));
+  *w = reinterpret_cast<unsigned int*>(b);
+  return WC_OK;
+}
+
 }  // namespace wc
 
 extern "C" int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int sense,
@@ -1329,10 +1208,10 @@ extern "C" int wc_dwt_device_noalloc(const void* in, void* out, int64_t len, int
   const int J = check_levels(len, nlevels, filter_len(filter));
   if (J == 0) return fail(WC_ERR_LEVELS, "nlevels %d invalid for length %lld", nlevels, (long long)len);
   if (!in || !out || in == out) return fail(WC_ERR_ARG, "in and out must be distinct device buffers");
-  unsigned char* base = nullptr;
-  WC_TRY(noalloc_base(&base));
   // No library stream is created here: NULL means the legacy default stream.
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char* base = nullptr;
+  WC_TRY(noalloc_base(&base, s, true));
   switch (precision) {
     case WC_F64_EXACT: return dispatch_noalloc<PExact>(in, out, len, sense, J, filter, s, base);
     case WC_F64_FAST: return dispatch_noalloc<PDD>(in, out, len, sense, J, filter, s, base);

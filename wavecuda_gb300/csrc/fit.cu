@@ -134,6 +134,7 @@ int wc_fit_thresholds(double* x, int64_t len, int nsig, int nlevels, int filter,
   if (!d) return workspace_error();
   WC_CUDA(cudaMemcpyAsync(d, x, bytes, cudaMemcpyHostToDevice, s));
   WC_TRY(fit_run(d, len, nsig, nlevels, filter, ttype, opts, results, s));
+  WC_TRY(take_status(s));  // x stays untouched when a wait gave up
   if (opts->smooth) {
     WC_CUDA(cudaMemcpyAsync(x, d, bytes, cudaMemcpyDeviceToHost, s));
     WC_CUDA(cudaStreamSynchronize(s));

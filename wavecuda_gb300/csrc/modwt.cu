@@ -32,102 +32,13 @@
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
 #include "wc_taps2.cuh"
+#include "wc_modwt_math.cuh"
+#include "wc_cvfused.h"
 
 namespace wc {
 namespace {
 
 constexpr int kThreads = 256;
-
-// Tap pairs of the packed double-float paths (wc_taps2.cuh): forward
-// (g_k, h_k); inverse (h_k, h_k) and (g_k, g_k).
-struct ModwtTapTable {
-  TapPairF f[8], h[8], g[8];
-};
-constexpr ModwtTapTable modwt_tap_table(int F) {
-  ModwtTapTable t{};
-  for (int k = 0; k < filter_len(F); k++) {
-    t.f[k] = tap_pair_f(tap_g(F, k), tap_h(F, k));
-    t.h[k] = tap_pair_f(tap_h(F, k), tap_h(F, k));
-    t.g[k] = tap_pair_f(tap_g(F, k), tap_g(F, k));
-  }
-  return t;
-}
-__constant__ ModwtTapTable kModwtTaps[5] = {ModwtTapTable{}, modwt_tap_table(1),
-                                            modwt_tap_table(2), modwt_tap_table(3),
-                                            modwt_tap_table(4)};
-
-// Forward analysis of one output from taps v[k * stride], k < L.
-template <int F, class P>
-__device__ __forceinline__ void fwd_taps(const typename P::V* v, int stride, typename P::V& s,
-                                         typename P::V& d) {
-  if constexpr (F == 1) {
-    s = haar_sum<P>(v[0], v[stride]);
-    d = haar_dif<P>(v[0], v[stride]);
-  } else if constexpr (std::is_same<P, PDD>::value) {
-    // d in lane 0, s in lane 1: the same operations as below, packed.
-    constexpr int L = filter_len(F);
-    dd_acc2 A = acc2_init(v[0], load_tap2(kModwtTaps[F].f[0]));
-#pragma unroll
-    for (int k = 1; k < L; k++) A = acc2_add(A, v[k * stride], load_tap2(kModwtTaps[F].f[k]));
-    acc2_fin(A, d, s);
-  } else {
-    constexpr int L = filter_len(F);
-    typename P::Acc ad = P::acc_init(v[0], tap_g(F, 0));
-    typename P::Acc as = P::acc_init(v[0], tap_h(F, 0));
-#pragma unroll
-    for (int k = 1; k < L; k++) {
-      ad = P::acc_add(ad, v[k * stride], tap_g(F, k));
-      as = P::acc_add(as, v[k * stride], tap_h(F, k));
-    }
-    d = P::acc_fin(ad);
-    s = P::acc_fin(as);
-  }
-}
-
-// Inverse synthesis of one output from S[-k * stride], D[-k * stride].
-template <int F, class P>
-__device__ __forceinline__ typename P::V inv_taps(const typename P::V* S, const typename P::V* D,
-                                                   int stride) {
-  if constexpr (F == 1) {
-    typename P::V acc = P::add(S[0], D[0]);
-    acc = P::add(acc, S[-stride]);
-    acc = P::sub(acc, D[-stride]);
-    return P::mul(acc, kHInvR2);
-  } else {
-    constexpr int L = filter_len(F);
-    typename P::Acc acc;
-#pragma unroll
-    for (int t = 0; t < L; t++) {
-      // even taps L-2, ..., 0 then odd taps L-1, ..., 1
-      const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
-      if (t == 0) acc = P::acc_init(S[-k * stride], tap_h(F, k));
-      else acc = P::acc_add(acc, S[-k * stride], tap_h(F, k));
-      acc = P::acc_add(acc, D[-k * stride], tap_g(F, k));
-    }
-    return P::half(P::acc_fin(acc));
-  }
-}
-
-// Two adjacent inverse outputs (S, D and S + 1, D + 1) in double-float with
-// packed pairs: per lane the operations of inv_taps, so the same bits.
-template <int F>
-__device__ __forceinline__ void inv_taps2_dd(const dd* S, const dd* D, int stride, dd& r0, dd& r1) {
-  constexpr int L = filter_len(F);
-  dd_acc2 A;
-#pragma unroll
-  for (int t = 0; t < L; t++) {
-    const int k = (t < L / 2) ? (L - 2 - 2 * t) : (L - 1 - 2 * (t - L / 2));
-    const tap2 h = load_tap2(kModwtTaps[F].h[k]), g = load_tap2(kModwtTaps[F].g[k]);
-    const dd* s = S - k * stride;
-    const dd* d = D - k * stride;
-    if (t == 0) A = acc2_init_xy(s[0], s[1], h);
-    else A = acc2_add_xy(A, s[0], s[1], h);
-    A = acc2_add_xy(A, d[0], d[1], g);
-  }
-  acc2_fin(A, r0, r1);
-  r0 = PDD::half(r0);
-  r1 = PDD::half(r1);
-}
 
 // Forward levels l0 .. l0+NF-1.  Tile: columns r0 .. r0+C-1, rows m0 ..
 // m0+M-1 of the row view with unit d0 = 2^l0 (nrows = n / d0 rows).
@@ -190,87 +101,14 @@ modwt_fwd_tiled(const typename P::T* __restrict__ X, typename P::T* __restrict__
   }
 }
 
-// Inverse levels l0+NI-1 down to l0 (row unit d0 = 2^l0).  Stop holds the
-// scaling sequence the group starts from (s block of level l0+NI-1, or the
-// previous group's output); the detail blocks come from xmod; out receives
-// the group's reconstruction for rows m0 .. m0+M-1.  Array row a of the tile
-// is global row m0 - HR + a (periodic).
+// Inverse levels l0+NI-1 down to l0 (row unit d0 = 2^l0); one CTA per tile
+// (modwt_inv_tile, wc_modwt_math.cuh).
 template <int F, class P, int NI>
 __global__ void __launch_bounds__(kThreads)
 modwt_inv_tiled(const typename P::T* __restrict__ Stop, const typename P::T* __restrict__ xmod,
                 typename P::T* __restrict__ out, int64_t n, int l0, int C, int M) {
-  using V = typename P::V;
-  constexpr int L = filter_len(F);
-  constexpr int HR = (L - 1) * ((1 << NI) - 1);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int R = M + HR;
-  V* St = reinterpret_cast<V*>(smem_raw);
-  V* Db = St + R * C;           // NI detail tiles
-  V* A = Db + NI * R * C;       // intermediates (NI > 1)
-  V* B = A + R * C;
-  const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
-  const int64_t nb = d0 / C;
-  const int64_t r0 = (blockIdx.x % nb) * C, m0 = (blockIdx.x / nb) * M;
-  const int cs = __ffs(C) - 1;
-  const int tot = R * C;
-  // Raw values arrive by per-thread asynchronous copies (every copy of the
-  // tile in flight at once), then each thread converts its own in place.
-  using T = typename P::T;
-  static_assert(sizeof(T) == sizeof(V), "in-place staging");
-  T* St_raw = reinterpret_cast<T*>(St);
-  T* Db_raw = reinterpret_cast<T*>(Db);
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-    const int row = e >> cs, c = e & (C - 1);
-    const int64_t g = (r0 + c) + ((m0 - HR + row) & (nrows - 1)) * d0;
-    cp_async_elem(St_raw + e, Stop + g);
-#pragma unroll
-    for (int t = 0; t < NI; t++)
-      cp_async_elem(Db_raw + t * tot + e, xmod + (int64_t)(2 * (l0 + t) + 1) * n + g);
-  }
-  cp_async_wait_all();
-  if constexpr (!std::is_same<T, V>::value) {
-    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-      St[e] = P::ld(St_raw[e]);
-#pragma unroll
-      for (int t = 0; t < NI; t++) Db[t * tot + e] = P::ld(Db_raw[t * tot + e]);
-    }
-  }
-  __syncthreads();
-  const V* cur = St;
-#pragma unroll
-  for (int t = NI - 1; t >= 0; t--) {
-    const int rd = 1 << t;
-    const int a_lo = HR - (L - 1) * ((1 << t) - 1);
-    V* dst = ((NI - 1 - t) & 1) ? B : A;
-    const V* Dt = Db + t * tot;
-    auto put = [&](int e, V v) {
-      if (t == 0) {
-        const int row = e >> cs, c = e & (C - 1);
-        out[(r0 + c) + (m0 - HR + row) * d0] = P::st(v);
-      } else {
-        dst[e] = v;
-      }
-    };
-    if constexpr (std::is_same<P, PDD>::value && F != 1) {
-      // outputs in adjacent pairs, one packed dot product per pair
-      const int e0 = a_lo * C;
-      int e = e0 + 2 * (int)threadIdx.x;
-      for (; e + 1 < tot; e += 2 * blockDim.x) {
-        V v0, v1;
-        inv_taps2_dd<F>(cur + e, Dt + e, rd * C, v0, v1);
-        put(e, v0);
-        put(e + 1, v1);
-      }
-      if (((tot - e0) & 1) && threadIdx.x == 0) put(tot - 1, inv_taps<F, P>(cur + tot - 1, Dt + tot - 1, rd * C));
-    } else {
-      for (int e = a_lo * C + threadIdx.x; e < tot; e += blockDim.x)
-        put(e, inv_taps<F, P>(cur + e, Dt + e, rd * C));
-    }
-    if (t > 0) {
-      __syncthreads();
-      cur = dst;
-    }
-  }
+  modwt_inv_tile<F, P, NI>(blockIdx.x, Stop, xmod, out, n, l0, C, M, smem_raw, NoDMap{});
 }
 
 template <class P>
@@ -436,6 +274,42 @@ int modwt(void* x, void* xmod, int64_t n, int sense, int J, int F, int prec, cud
     case WC_F64_EXACT: return dispatch_modwt<PExact>(x, xmod, n, sense, J, F, s);
     case WC_F64_FAST: return dispatch_modwt<PDD>(x, xmod, n, sense, J, F, s);
     case WC_F32: return dispatch_modwt<PF32>(x, xmod, n, sense, J, F, s);
+  }
+  return fail(WC_ERR_ARG, "unknown precision %d", prec);
+}
+
+namespace {
+template <class P>
+int inv_groups_p(int64_t n, int J, int F, int target, CvModGroup* out, int* ngroups,
+                 size_t* smem_max) {
+  const int L = filter_len(F);
+  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+  const int nimax = F == 1 ? 3 : 2;
+  int g = 0;
+  size_t smax = 0;
+  for (int hi = J - 1; hi >= 0; g++) {
+    if (g >= kCvMaxGroups) return fail(WC_ERR_ARG, "too many MODWT level groups");
+    const int ni = std::min(nimax, hi + 1);
+    const int l0 = hi - ni + 1;
+    const int HR = (L - 1) * ((1 << ni) - 1);
+    const Geo<P> geo = tile_geo<P>(n, l0, HR, 2 * ni, 0, target > 0 ? target : mc.inv_target,
+                                   (size_t)mc.inv_smem_kb * 1024);
+    out[g] = CvModGroup{l0, ni, geo.C, geo.M, (((int64_t)1 << l0) / geo.C) * ((n >> l0) / geo.M)};
+    smax = std::max(smax, geo.smem);
+    hi = l0 - 1;
+  }
+  *ngroups = g;
+  *smem_max = smax;
+  return WC_OK;
+}
+}  // namespace
+
+int modwt_inv_groups(int64_t n, int J, int F, int prec, int target, CvModGroup* out,
+                     int* ngroups, size_t* smem_max) {
+  switch (prec) {
+    case WC_F64_EXACT: return inv_groups_p<PExact>(n, J, F, target, out, ngroups, smem_max);
+    case WC_F64_FAST: return inv_groups_p<PDD>(n, J, F, target, out, ngroups, smem_max);
+    case WC_F32: return inv_groups_p<PF32>(n, J, F, target, out, ngroups, smem_max);
   }
   return fail(WC_ERR_ARG, "unknown precision %d", prec);
 }

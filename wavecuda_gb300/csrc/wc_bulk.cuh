@@ -7,8 +7,10 @@
 // bounded: after kMaxPolls unsuccessful polls the waiting thread records a
 // timeout in the device status word (read with wc_device_status) and the
 // kernel skips its work instead of hanging the GPU.  The status word lives in
-// the library workspace (wc::device_status_word) and is read back with
-// wc_device_status().
+// the library workspace (wc::device_status_word); every host-buffer call reads
+// and clears it after its work and returns WC_ERR_TIMEOUT when the bit is
+// set, and wc_device_status() reads it for the asynchronous device-pointer
+// calls.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -47,10 +49,13 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
       : "memory");
 }
 
-// Bounded wait for phase `parity` of `bar`; false when it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned int* status) {
+// Bounded wait for phase `parity` of `bar`; false when it gave up after
+// max_polls unsuccessful polls (each poll may suspend the thread for a short,
+// hardware-defined time).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned int* status,
+                                          unsigned int max_polls = kMaxPolls) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned int it = 0; it < kMaxPolls; it++) {
+  for (unsigned int it = 0; it < max_polls; it++) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -63,6 +68,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsign
   }
   if (status) atomicOr(status, kStatusTimeout);
   return false;
+}
+
+// Invalidates an mbarrier whose shared memory is about to be reused.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // Makes this thread's generic-proxy shared-memory writes visible to the

@@ -81,6 +81,20 @@ int workspace_error();  // WC_ERR_NOMEM / WC_ERR_CUDA of the last workspace() fa
 // Per-device status word that kernels OR error bits into (bit 0: a bounded
 // device-side wait gave up); zero-initialised when first created.
 unsigned int* device_status_word();
+// The same word if it already exists on the current device (nullptr
+// otherwise); never allocates.
+unsigned int* existing_status_word();
+// Synchronises s, then reads and clears the status word: WC_ERR_TIMEOUT (with
+// the error text set) when a bounded wait gave up, else WC_OK.  Every
+// host-buffer call runs it after its device work and before it writes the
+// caller's buffers.
+int take_status(cudaStream_t s);
+// Status word of the allocation-free DWT (inside its static device array) on
+// the current device: the _if_known form returns nullptr until that entry
+// point has looked the array up on this device and never calls the runtime's
+// symbol lookup; noalloc_status_word looks it up.
+unsigned int* noalloc_status_word_if_known();
+int noalloc_status_word(unsigned int** w);
 
 // The library's own non-blocking stream on the current device.
 cudaStream_t lib_stream();

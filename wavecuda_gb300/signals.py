@@ -8,6 +8,10 @@
 * ``blocks_like``, ``bumps_like``, ``heavisine_like`` -- this project's own
   piecewise test shapes (step functions, sharp peaks, a sinusoid with jumps),
   generated from a seed; they are not the Donoho-Johnstone test functions.
+* ``batch_workload`` -- the batched-smoothing workload: signals of length
+  2^k, k uniform on {kmin..kmax}, random filter and transform, levels
+  min(k, 10) clamped to the filter's maximum, universal or CV soft
+  thresholds, shapes above at SNR 3 or 7, back to back in one array.
 
 All generators are deterministic given (n, seed) and use numpy's PCG64.
 """
@@ -74,3 +78,28 @@ def roofline_input(n: int, seed: int = 0) -> np.ndarray:
         ph = rng.uniform(0, 2 * np.pi)
         x += np.sin(2 * np.pi * fr * i / n + ph)
     return x
+
+
+def batch_workload(nsig: int, seed: int, max_levels, kmin: int = 10, kmax: int = 20):
+    """(data, specs, clean): `specs` holds one dict per signal with the
+    fields of a wc_signal record (offset, len, nlevels, ttype, filter,
+    threshtype, hardness, minlevel, maxlevel, thresh, tol); max_levels(n,
+    filter) is the level limit (check_len_levels)."""
+    rng = np.random.default_rng(seed)
+    shapes = list(SHAPES)
+    specs, chunks, clean, off = [], [], [], 0
+    for i in range(nsig):
+        k = int(rng.integers(kmin, kmax + 1))
+        n = 1 << k
+        filt = int(rng.integers(1, 5))
+        ttype = int(rng.integers(0, 2))
+        J = min(k, 10, max_levels(n, filt))
+        tt = int(rng.choice([1, 2]))  # universal or cross-validated
+        f = SHAPES[shapes[int(rng.integers(0, 4))]](n, i)
+        x = noisy(f, float(rng.choice([3.0, 7.0])), seed=seed * 7919 + i)
+        chunks.append(x)
+        clean.append(f)
+        specs.append(dict(offset=off, len=n, nlevels=J, ttype=ttype, filter=filt, threshtype=tt,
+                          hardness=1, minlevel=0, maxlevel=J - 1, thresh=0.0, tol=1e-8))
+        off += n
+    return np.concatenate(chunks), specs, np.concatenate(clean)
