@@ -624,8 +624,17 @@ def smooth_bench(wc, args):
     """GPUSmooth plain (exact FP64) against its precision forms: MODWT Haar
     and LA8, 10 levels, soft, two-fold CV (golden section, tol 1e-8), levels
     1..10 (0..9 in C), n = 2^20 signals shaped like doppler/blocks/bumps/
-    heavisine at SNR 3 and 7; one wc_smooth call per signal."""
+    heavisine at SNR 3 and 7; one wc_smooth call per signal (host arrays).
+    The golden search runs as one cooperative launch (cv_fused_search); its
+    live device time over the search's loss evaluations (iterations + 2)
+    gives the time per golden step and its HBM fraction for the step's
+    algorithmic bytes: two half-length inverse MODWTs (J = 9: read s_9 and
+    d_1..d_9, write the reconstruction) and the loss pass (read both
+    reconstructions and the signal)."""
+    import ctypes as C
     from wavecuda_gb300 import signals as sg
+    L = wc.lib()
+    hbm, _ = peaks()
     n, J = 1 << args.smooth_log2n, 10
     sigs = []
     for i, shape in enumerate(sg.SHAPES):
@@ -638,6 +647,8 @@ def smooth_bench(wc, args):
         ref_t = None
         for prec in (0, 1, 2):
             ts, mses, ths, its = [], [], [], []
+            wc.smooth(sigs[0][1], J, wc.MODWT, filt, wc.CV, 0.0, wc.SOFT, 0, J - 1, 1e-8, prec)
+            L.wc_profile_start()
             for f, x in sigs:
                 t0 = time.perf_counter()
                 y, info = wc.smooth(x, J, wc.MODWT, filt, wc.CV, 0.0, wc.SOFT, 0, J - 1, 1e-8, prec)
@@ -645,13 +656,27 @@ def smooth_bench(wc, args):
                 mses.append(float(np.mean((y - f) ** 2)))
                 ths.append(info.thresh)
                 its.append(info.cv_iterations)
+            arr = (KernelTime * 64)()
+            cnt = C.c_int()
+            L.wc_profile_stop(arr, 64, C.byref(cnt))
+            prof = {arr[i].name.decode(): arr[i].total_ms for i in range(cnt.value)}
             if prec == 0:
                 ref_t = ths
-            out[f"{fname}/{PREC[prec]}"] = {
-                "signals_s": len(sigs) / sum(ts), "ms_per_signal": 1e3 * sum(ts) / len(sigs),
-                "mse_vs_clean": float(np.mean(mses)), "cv_iterations": float(np.mean(its)),
-                "thresh_rel_diff_vs_exact": float(max(abs(a - b) / abs(b)
-                                                      for a, b in zip(ths, ref_t)))}
+            es = 4 if prec == 2 else 8
+            h = n // 2
+            step_b = 2 * (J - 1 + 2) * h * es + 2 * h * es + 8 * n
+            steps = sum(its) + 2 * len(sigs)
+            r = {"signals_s": len(sigs) / sum(ts), "ms_per_signal": 1e3 * sum(ts) / len(sigs),
+                 "mse_vs_clean": float(np.mean(mses)), "cv_iterations": float(np.mean(its)),
+                 "thresh_rel_diff_vs_exact": float(max(abs(a - b) / abs(b)
+                                                       for a, b in zip(ths, ref_t)))}
+            if "cv_fused_search" in prof:
+                us = prof["cv_fused_search"] * 1e3 / steps
+                r["search_ms_per_signal"] = prof["cv_fused_search"] / len(sigs)
+                r["us_per_golden_step"] = us
+                r["golden_step_bytes"] = step_b
+                r["golden_step_hbm_frac"] = step_b / (us * 1e-6) / 1e9 / hbm
+            out[f"{fname}/{PREC[prec]}"] = r
     return out
 
 

@@ -7,10 +7,12 @@
 // with J-1 levels, and a golden-section search over t in [0, t_univ] keeps
 // two candidates t1 < t2.  Each new candidate thresholds both halves (levels
 // [minlevel, maxlevel-1]), inverts them and scores the interpolation error
-// of thresh.cpp:344-385.  All of that runs on the device; only the scalar
-// loss comes back to drive the search, which is the reference's own FP64
-// host logic (constants R = 0.61803399, at most 51 iterations, final
-// rescale t / sqrt(1 - ln 2 / ln n)).
+// of thresh.cpp:344-385.  For the DWT and the time-ordered MODWT the whole
+// search runs on the device in one persistent cooperative launch
+// (cv_fused_kernel.cuh): no host round trip per step.  The packet-ordered
+// MODWT keeps the step-by-step form, where only the scalar loss comes back
+// to drive the reference's FP64 host logic.  Constants R = 0.61803399, at
+// most 51 iterations, final rescale t / sqrt(1 - ln 2 / ln n).
 //
 // Bit-exact selection.  With soft thresholds the two losses compared in the
 // last iterations differ by ~1e-16 relative, below rounding noise, so the
@@ -31,10 +33,14 @@
 //    transform refuses to run (transform.cpp:5-8); the work vectors then stay
 //    zero, and so they do here.
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 
 #include <algorithm>
 
 #include "wc_common.cuh"
+#include "wc_cvfused.h"
+#include "wc_grid.cuh"
 
 namespace wc {
 
@@ -169,6 +175,135 @@ int loss(const Ctx<T>& c, const HalfVec<T>& ye, const HalfVec<T>& yo, const doub
   return WC_OK;
 }
 
+// The golden-section search of CVT (thresh.cpp:249-320) in one cooperative
+// launch: wec / woc are the transformed halves; returns the chosen threshold
+// before the final rescale, the iteration count and the smallest relative
+// loss margin.  Synchronous (the result comes back to the host).
+template <class T>
+int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x, double t_univ,
+                    double tol, double* t_out, int* iters, double* min_margin) {
+  const int64_t lenh = c.lenh;
+  const int J1 = c.J - 1;
+  const int L = filter_len(c.F);
+  const int64_t Cn = (lenh + 1023) / 1024;
+  const int64_t ntop = lenh >> J1;
+  auto al = [](size_t b) { return ((b + 255) / 256) * 256; };
+  const size_t b_rec = al(sizeof(T) * (size_t)lenh), b_top = al(sizeof(T) * (size_t)ntop);
+  const size_t b_bar = 16384;  // barrier words (grid_bar_words), the phase timer in the last 1 KB
+  const size_t b_zero = al(sizeof(CvFusedState)) + b_bar + 4 * b_rec + 4 * b_top;
+  const size_t need = b_zero + 4 * b_rec + al(sizeof(double) * (size_t)lenh) +
+                      al(sizeof(double) * (size_t)Cn) + al(sizeof(int) * (size_t)Cn) +
+                      al(sizeof(long long) * 32 * (size_t)Cn) +
+                      al(sizeof(long long) * 16 * 32 * (size_t)Cn);
+  char* base = static_cast<char*>(workspace(kSlotCvTerms, need));
+  if (!base) return workspace_error();
+  CvFusedArgs a{};
+  size_t off = 0;
+  a.st = reinterpret_cast<CvFusedState*>(base);
+  off += al(sizeof(CvFusedState));
+  a.bar = reinterpret_cast<unsigned int*>(base + off);
+  off += b_bar;
+  for (int k = 0; k < 4; k++, off += b_rec) a.rec[k] = base + off;
+  for (int k = 0; k < 4; k++, off += b_top) a.top[k] = base + off;
+  // off == b_zero: everything above starts at zero
+  for (int h = 0; h < 2; h++)
+    for (int k = 0; k < 2; k++, off += b_rec) a.tmp[h][k] = base + off;
+  a.terms = reinterpret_cast<double*>(base + off);
+  off += al(sizeof(double) * (size_t)lenh);
+  a.chunk_s = reinterpret_cast<double*>(base + off);
+  off += al(sizeof(double) * (size_t)Cn);
+  a.chunk_e = reinterpret_cast<int*>(base + off);
+  off += al(sizeof(int) * (size_t)Cn);
+  a.chunk_q = reinterpret_cast<long long*>(base + off);
+  off += al(sizeof(long long) * 32 * (size_t)Cn);
+  a.sub_q = reinterpret_cast<long long*>(base + off);
+  a.wcoef[0] = wec;
+  a.wcoef[1] = woc;
+  a.x = x;
+  a.status = device_status_word();
+  if (!a.status) return workspace_error();
+  a.lenh = lenh;
+  a.J1 = J1;
+  a.minl = c.minl;
+  a.maxl1 = c.maxl - 1;
+  a.hardness = c.hardness;
+  a.thr_on = range_ok(lenh, J1, c.minl, c.maxl - 1, L) ? 1 : 0;
+  a.tol = tol;
+  // Search start (thresh.cpp:249-260), in the reference's FP64 order.
+  const double R = 0.61803399, C = 1. - R;
+  const double ta = 0., tc = t_univ, tb = tc / 2.;
+  CvFusedState st0{};
+  st0.t0 = ta;
+  st0.t2 = tb;
+  st0.t1 = tb - C * (tb - ta);
+  st0.t3 = tc;
+  int dev = 0, sms = 1, coop = 0;
+  WC_CUDA(cudaGetDevice(&dev));
+  WC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  WC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return fail(WC_ERR_UNSUPPORTED, "device without cooperative launch");
+  // Dynamic shared memory: the replay's staging (1024 chunks' candidate
+  // increments and binades, one chunk's terms and its sub-chunk windows),
+  // the MODWT tiles or the DWT coarse levels (two buffers of kCvCoarseMax).
+  size_t smem = (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) + 1024 * sizeof(double) +
+                16 * 32 * sizeof(long long);
+  const size_t vsize = (c.prec == WC_F32) ? 4 : 8;
+  if (c.ttype == 1) {
+    // Tiles small enough that both halves give every CTA (about three per
+    // SM) two or more of them, but at least 512 values (the halo rows grow
+    // with the fused levels).
+    int target = (c.prec == WC_F32) ? 4096 : 2048;
+    while (target > 512 && 2 * lenh / target < (int64_t)6 * sms) target >>= 1;
+    size_t gs = 0;
+    WC_TRY(modwt_inv_groups(lenh, J1, c.F, c.prec, target, a.grp, &a.ngroups, &gs));
+    smem = std::max(smem, gs);
+  } else {
+    int lc = 0;
+    while ((lenh >> lc) > kCvCoarseMax) lc++;
+    a.dwt_lc = lc;
+    if (lc <= J1 - 1) smem = std::max(smem, 2 * (size_t)kCvCoarseMax * vsize);
+  }
+  int per = 0;
+  switch (c.prec) {
+    case WC_F64_EXACT: per = cv_fused_occupancy_exact(c.F, c.ttype, smem); break;
+    case WC_F64_FAST: per = cv_fused_occupancy_fast(c.F, c.ttype, smem); break;
+    default: per = cv_fused_occupancy_f32(c.F, c.ttype, smem); break;
+  }
+  if (per < 1) return fail(WC_ERR_CUDA, "fused CV search: no resident CTA at %zu bytes", smem);
+  const int grid = std::max(2, per * sms);
+  if (sizeof(unsigned int) * grid_bar_words((unsigned)grid) > b_bar - 1024)
+    return fail(WC_ERR_UNSUPPORTED, "fused CV search: grid of %d CTAs too large", grid);
+  WC_CUDA(cudaMemsetAsync(base, 0, b_zero, c.s));
+  // WAVECUDA_CV_TRACE=1: print the search's time per phase to stderr.
+  static const bool trace_on = getenv("WAVECUDA_CV_TRACE") != nullptr;
+  if (trace_on)
+    a.trace = reinterpret_cast<unsigned long long*>(base + al(sizeof(CvFusedState)) + b_bar - 1024);
+  WC_CUDA(cudaMemcpyAsync(a.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, c.s));
+  int r = WC_OK;
+  switch (c.prec) {
+    case WC_F64_EXACT: r = cv_fused_launch_exact(a, c.F, c.ttype, grid, smem, c.s); break;
+    case WC_F64_FAST: r = cv_fused_launch_fast(a, c.F, c.ttype, grid, smem, c.s); break;
+    default: r = cv_fused_launch_f32(a, c.F, c.ttype, grid, smem, c.s); break;
+  }
+  WC_TRY(r);
+  CvFusedState st{};
+  WC_CUDA(cudaMemcpyAsync(&st, a.st, sizeof(st), cudaMemcpyDeviceToHost, c.s));
+  WC_CUDA(cudaStreamSynchronize(c.s));
+  if (a.trace) {
+    unsigned long long tr[kCvTraceSlots];
+    WC_CUDA(cudaMemcpy(tr, a.trace, sizeof(tr), cudaMemcpyDeviceToHost));
+    fprintf(stderr, "cv_fused_search phases (us, %d steps, grid %d, smem %zu):", st.iters + 2,
+            grid, smem);
+    for (int k = 0; k < kCvTraceSlots; k++)
+      if (tr[k]) fprintf(stderr, " [%d] %.1f", k, tr[k] * 1e-3);
+    fprintf(stderr, "\n");
+  }
+  *t_out = st.m1 < st.m2 ? st.t1 : st.t2;
+  *iters = st.iters;
+  *min_margin = st.min_margin;
+  return WC_OK;
+}
+
 // Carves `count` buffers out of one workspace slot.
 struct Carver {
   char* base;
@@ -199,7 +334,8 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
   // Workspace: full-length signal (T), full transform, and for CV the
   // half-length vectors.
   size_t need = 256 * 32 + sizeof(T) * (size_t)(n + wlen);
-  if (threshtype == 2) need += sizeof(T) * (size_t)(2 * lenh + 2 * hlen + 4 * (2 * lenh + hlen));
+  if (threshtype == 2)
+    need += sizeof(T) * (size_t)(2 * lenh + 2 * hlen + (po ? 4 * (2 * lenh + hlen) : 0));
   need += sizeof(double) * (size_t)wlen;  // FP64 copy of an FP32 transform (univ/counts)
   Carver cv{static_cast<char*>(workspace(kSlotCv, need)), 0};
   if (!cv.base) return workspace_error();
@@ -238,25 +374,6 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
     T* wo = cv.take<T>(lenh);
     T* wec = cv.take<T>(hlen);
     T* woc = cv.take<T>(hlen);
-    HalfVec<T> y[4];
-    for (int k = 0; k < 4; k++) {
-      y[k].buf[0] = cv.take<T>(lenh);
-      y[k].buf[1] = cv.take<T>(lenh);
-      y[k].mod = cv.take<T>(hlen);
-      y[k].cur = 0;
-      y[k].transformed = 0;
-    }
-    // Zero the work vectors: the reference's are fresh zero-filled pages.
-    WC_CUDA(cudaMemsetAsync(y[0].buf[0], 0,
-                            (size_t)(reinterpret_cast<char*>(y[3].mod + hlen) -
-                                     reinterpret_cast<char*>(y[0].buf[0])), s));
-    const size_t tbytes = ((sizeof(double) * (size_t)(lenh + 64) + 255) / 256) * 256;
-    char* tbase = static_cast<char*>(workspace(kSlotCvTerms, tbytes + cv_sum_scratch_bytes(lenh)));
-    if (!tbase) return workspace_error();
-    double* terms = reinterpret_cast<double*>(tbase);
-    double* dsum = terms + lenh + 32;
-    void* sscr = tbase + tbytes;
-
     split_even_odd<T><<<grid_for(lenh), kThreads, 0, s>>>(x, lenh, we, wo);
     WC_TRY(after_launch("split_even_odd"));
     WC_TRY(transform_full(c, xt, w, n, J, 1));
@@ -264,38 +381,60 @@ int smooth_impl(double* x, int64_t n, int J, int ttype, int F, int threshtype, d
     if (!wd) return WC_ERR_CUDA;
     WC_TRY(univ_thresh(wd, n, J, ttype, minl, maxl, s, &t_univ));
 
-    const double R = 0.61803399, C = 1. - R;
-    double ta = 0., tc = t_univ;
-    double tb = tc / 2.;
-    double t0 = ta, t2 = tb, t1 = tb - C * (tb - ta), t3 = tc;
     WC_TRY(transform_full(c, we, wec, lenh, lv1, 1));
     WC_TRY(transform_full(c, wo, woc, lenh, lv1, 1));
-    WC_TRY(half_step(c, wec, y[0], t1));
-    WC_TRY(half_step(c, woc, y[1], t1));
-    WC_TRY(half_step(c, wec, y[2], t2));
-    WC_TRY(half_step(c, woc, y[3], t2));
-    double m1, m2;
-    WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
-    WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
-    while (fabs(t3 - t0) > tol * (t1 + t2)) {
-      if (iters > 50) break;
-      if (m1 != 0.0) min_margin = std::min(min_margin, fabs(m1 - m2) / fabs(m1));
-      if (m2 < m1) {
-        t0 = t1; t1 = t2; t2 = R * t2 + C * t3;
-        m1 = m2;
-        WC_TRY(half_step(c, wec, y[2], t2));
-        WC_TRY(half_step(c, woc, y[3], t2));
-        WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
-      } else {
-        t3 = t2; t2 = t1; t1 = R * t1 + C * t0;
-        m2 = m1;
-        WC_TRY(half_step(c, wec, y[0], t1));
-        WC_TRY(half_step(c, woc, y[1], t1));
-        WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
+    if (!po) {
+      WC_TRY(cv_search_fused<T>(c, wec, woc, x, t_univ, tol, &t, &iters, &min_margin));
+    } else {
+      HalfVec<T> y[4];
+      for (int k = 0; k < 4; k++) {
+        y[k].buf[0] = cv.take<T>(lenh);
+        y[k].buf[1] = cv.take<T>(lenh);
+        y[k].mod = cv.take<T>(hlen);
+        y[k].cur = 0;
+        y[k].transformed = 0;
       }
-      iters++;
+      // Zero the work vectors: the reference's are fresh zero-filled pages.
+      WC_CUDA(cudaMemsetAsync(y[0].buf[0], 0,
+                              (size_t)(reinterpret_cast<char*>(y[3].mod + hlen) -
+                                       reinterpret_cast<char*>(y[0].buf[0])), s));
+      const size_t tbytes = ((sizeof(double) * (size_t)(lenh + 64) + 255) / 256) * 256;
+      char* tbase = static_cast<char*>(workspace(kSlotCvTerms, tbytes + cv_sum_scratch_bytes(lenh)));
+      if (!tbase) return workspace_error();
+      double* terms = reinterpret_cast<double*>(tbase);
+      double* dsum = terms + lenh + 32;
+      void* sscr = tbase + tbytes;
+      const double R = 0.61803399, C = 1. - R;
+      double ta = 0., tc = t_univ;
+      double tb = tc / 2.;
+      double t0 = ta, t2 = tb, t1 = tb - C * (tb - ta), t3 = tc;
+      WC_TRY(half_step(c, wec, y[0], t1));
+      WC_TRY(half_step(c, woc, y[1], t1));
+      WC_TRY(half_step(c, wec, y[2], t2));
+      WC_TRY(half_step(c, woc, y[3], t2));
+      double m1, m2;
+      WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
+      WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
+      while (fabs(t3 - t0) > tol * (t1 + t2)) {
+        if (iters > 50) break;
+        if (m1 != 0.0) min_margin = std::min(min_margin, fabs(m1 - m2) / fabs(m1));
+        if (m2 < m1) {
+          t0 = t1; t1 = t2; t2 = R * t2 + C * t3;
+          m1 = m2;
+          WC_TRY(half_step(c, wec, y[2], t2));
+          WC_TRY(half_step(c, woc, y[3], t2));
+          WC_TRY(loss(c, y[2], y[3], x, terms, dsum, sscr, &m2));
+        } else {
+          t3 = t2; t2 = t1; t1 = R * t1 + C * t0;
+          m2 = m1;
+          WC_TRY(half_step(c, wec, y[0], t1));
+          WC_TRY(half_step(c, woc, y[1], t1));
+          WC_TRY(loss(c, y[0], y[1], x, terms, dsum, sscr, &m1));
+        }
+        iters++;
+      }
+      t = m1 < m2 ? t1 : t2;
     }
-    t = m1 < m2 ? t1 : t2;
     t = t / (sqrt(1. - log(2.) / log((double)n)));
   } else {
     WC_TRY(transform_full(c, xt, w, n, J, 1));

@@ -36,10 +36,11 @@ struct CvFusedArgs {
   void* tmp[2][2];       // intermediate scaling sequences per half (T, lenh each)
   double* terms;         // lenh loss terms
   double* chunk_s;       // per chunk of kSeqChunk terms: FP64 sum (any order)
-  int* chunk_e;          // binade estimate of the running sum at the chunk's start
-  long long* chunk_q;    // 3 per chunk
+  int* chunk_e;          // per chunk: e0, the lowest binade above all its terms
+  long long* chunk_q;    // per chunk: integer increments for the binades e0 .. e0+31
+  long long* sub_q;      // per chunk: the same for its 16 sub-chunks of 64 terms
   CvFusedState* st;
-  unsigned int* bar;     // grid barrier (2 words, zero)
+  unsigned int* bar;     // grid barrier words (grid_bar_words, zero)
   unsigned int* status;  // status word (bit 0: a bounded wait gave up)
   int64_t lenh;
   int J1;                // levels of the half-length transforms
@@ -50,7 +51,14 @@ struct CvFusedArgs {
   int ngroups;           // MODWT inverse groups, coarsest first
   CvModGroup grp[kCvMaxGroups];
   int dwt_lc;            // DWT: levels J1-1 .. dwt_lc run in one CTA per half (dwt_lc > J1-1: none)
+  // Optional phase timer (nullptr: off): CTA 0 adds the wall time (ns) of
+  // each phase over the whole search, slots 0 .. kCvMaxGroups-1 for the
+  // transform's level groups (DWT: 0 = the coarse CTA phase, 1 + k = fine
+  // level k), then the loss terms and the replay.
+  unsigned long long* trace;
 };
+constexpr int kCvTraceTerms = kCvMaxGroups, kCvTraceReplay = kCvMaxGroups + 1,
+              kCvTraceSlots = kCvMaxGroups + 2;
 
 // Level groups of the time-ordered MODWT inverse of an n-sample signal with
 // J levels, coarsest first, as the tiled inverse runs them (tile target
@@ -61,7 +69,8 @@ int modwt_inv_groups(int64_t n, int J, int F, int prec, int target, CvModGroup* 
 
 // Per-precision instantiations (cv_fused_exact.cu, cv_fused_fast.cu,
 // cv_fused_f32.cu): cooperative launch of the search for filter F and
-// transform ttype (0 DWT, 1 MODWT); smem/grid from cv_fused_geometry.
+// transform ttype (0 DWT, 1 MODWT) on `grid` CTAs with `smem` bytes of
+// dynamic shared memory.
 int cv_fused_launch_exact(const CvFusedArgs& a, int F, int ttype, int grid, size_t smem,
                           cudaStream_t s);
 int cv_fused_launch_fast(const CvFusedArgs& a, int F, int ttype, int grid, size_t smem,
