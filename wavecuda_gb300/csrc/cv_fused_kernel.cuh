@@ -16,15 +16,16 @@
 //       MODWT  row-view tiles of up to three levels (modwt_inv_tile);
 //       DWT    the coarse levels (at most kCvCoarseMax outputs) in one CTA per
 //              half, then one grid-wide pass per finer level;
-//  2. the interpolation loss terms of interp_mse (thresh.cpp:344-385), their
-//     per-chunk FP64 sums, and per chunk and 64-term sub-chunk the integer
-//     increments of the exact serial sum for a window of 32 binades
-//     (wc_seqsum.cuh); CTA 0 also replays the first chunk, which depends on
-//     nothing else;
-//  3. CTA 0 finds each chunk's binade from the FP64 prefix of the chunk sums
-//     and one warp replays the reference's left-to-right FP64 sum exactly
-//     (walking the chunks, replaying only sub-chunks with a binade crossing
-//     or a tie); every CTA reads the loss after the next barrier.
+//  2. the interpolation loss terms of interp_mse (thresh.cpp:344-385) and
+//     their per-chunk FP64 sums; CTA 0 also replays the first chunk, which
+//     depends on nothing else;
+//  3. per chunk, the binade of the running sum at its start (from the FP64
+//     prefix of the chunk sums) and the integer increments of the chunk and
+//     of its 64-term sub-chunks for the three candidate binades
+//     (wc_seqsum.cuh);
+//  4. one warp of CTA 0 replays the reference's left-to-right FP64 sum
+//     exactly (walking the chunks, replaying only sub-chunks with a binade
+//     crossing or a tie); every CTA reads the loss after the next barrier.
 //
 // Quirks kept (they change results): DWT work vectors keep the previous
 // reconstruction in their coarse scaling slots k 2^J1, k > 0, because
@@ -53,7 +54,7 @@ constexpr int kCvSeg = 1024;  // chunks staged in shared memory by the replaying
 // segment's candidate increments and binades, one chunk's terms and its
 // sub-chunk windows.
 constexpr size_t kCvSeqSmem = (size_t)kCvSeg * (3 * sizeof(long long) + sizeof(int)) +
-                              kSeqChunk * sizeof(double) + kSeqSubs * kSeqWin * sizeof(long long);
+                              kSeqChunk * sizeof(double) + kSeqSubs * 3 * sizeof(long long);
 
 // thresh_coef (thresh.cpp:142-157) on an FP64 value, bit-identical to
 // `fabs(c) < t ? 0 : soft ? sign(c) * (fabs(c) - t) : c` with IEEE roundings:
@@ -158,8 +159,8 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
   using V = typename P::V;
   constexpr int HH = filter_len(F) / 2;
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ long long s_sub[kSeqSubs * 3];
   __shared__ double s_wd[32];
-  __shared__ int s_we[32];
   __shared__ unsigned long long s_m0;
 
   unsigned int gen = 0;
@@ -301,62 +302,44 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
     else return modwt_step(t, pair);
   };
 
-  // ---- 2-3. loss of a pair of reconstructions ----------------------------
+  // ---- 2-4. loss of a pair of reconstructions ----------------------------
   auto loss = [&](int pair, double& m) -> bool {
     const T* ye = static_cast<const T*>(a.rec[2 * pair]);
     const T* yo = static_cast<const T*>(a.rec[2 * pair + 1]);
     const int64_t Cn = (lenh + kSeqChunk - 1) / kSeqChunk;
-    // (2) each chunk's terms, FP64 sum, and integer increments for the 32
-    //     binades above its largest term, per 64-term sub-chunk and in all
-    double* sT = reinterpret_cast<double*>(smem);
-    long long* sW = reinterpret_cast<long long*>(sT + kSeqChunk);
+    // (2) the terms and per-chunk FP64 sums
+    double* s_chunk0 = reinterpret_cast<double*>(smem);  // CTA 0: the first chunk's terms
     for (int64_t c = blockIdx.x; c < Cn; c += gridDim.x) {
       const int64_t base = c * kSeqChunk;
       const int len = (int)(lenh - base < kSeqChunk ? lenh - base : kSeqChunk);
       double acc = 0.0;
-      int emax = 0;
       for (int k = threadIdx.x; k < len; k += blockDim.x) {
         const double v = cv_term(ye, yo, a.x, lenh, base + k);
         a.terms[base + k] = v;
-        sT[k] = v;
+        if (c == 0) s_chunk0[k] = v;
         acc += v;
-        emax = max(emax, (int)(((unsigned long long)__double_as_longlong(v) >> 52) & 0x7FF));
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        acc += __shfl_down_sync(0xffffffffu, acc, o);
-        emax = max(emax, __shfl_down_sync(0xffffffffu, emax, o));
-      }
-      if ((threadIdx.x & 31) == 0) {
-        s_wd[threadIdx.x >> 5] = acc;
-        s_we[threadIdx.x >> 5] = emax;
-      }
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if ((threadIdx.x & 31) == 0) s_wd[threadIdx.x >> 5] = acc;
       __syncthreads();
       if (threadIdx.x == 0) {
         double t = 0.0;
-        int e = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-          t += s_wd[w];
-          e = max(e, s_we[w]);
-        }
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_wd[w];
         a.chunk_s[c] = t;
-        a.chunk_e[c] = e + 1;
-        s_we[0] = e + 1;
       }
       __syncthreads();
-      const int e0 = s_we[0];
-      seq_window_q(sT, len, e0, sW, a.sub_q + (int64_t)kSeqSubs * kSeqWin * c,
-                   a.chunk_q + (int64_t)kSeqWin * c);
-      if (c == 0) {
-        // The first chunk starts from m = 0 and crosses many binades; it
-        // needs nothing from the other chunks, so CTA 0 replays it now, from
-        // shared memory, while the other CTAs compute.
-        if (threadIdx.x < 32) {
-          unsigned long long mb = 0ull;
-          seq_replay_chunk_warp(sT, len, nullptr, 0, mb);
-          if (threadIdx.x == 0) s_m0 = mb;
-        }
-        __syncthreads();
+    }
+    if (blockIdx.x == 0) {
+      // The first chunk starts from m = 0 and crosses many binades; it needs
+      // nothing from the other chunks, so CTA 0 replays it now (from shared
+      // memory), while the other CTAs compute their terms.
+      if (threadIdx.x < 32) {
+        unsigned long long mb = 0ull;
+        const int len0 = (int)(lenh < kSeqChunk ? lenh : kSeqChunk);
+        seq_replay_chunk_warp(s_chunk0, len0, nullptr, 0, mb);
+        if (threadIdx.x == 0) s_m0 = mb;
       }
+      __syncthreads();
     }
     if constexpr (TT == 0) {
       // the coarse slots of this pair's reconstructions, for its next step
@@ -371,40 +354,44 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
     }
     if (!grid_sync(a.bar, nb, gen, a.status)) return false;
     mark(kCvTraceTerms);
-    // (3) CTA 0: the binade of the running sum at each chunk's start is that
-    //     of the FP64 prefix of the chunk sums or a neighbour; one warp walks
-    //     the chunks with the matching increments and replays, sub-chunk by
-    //     sub-chunk, the few it cannot pass (binade crossings, ties).
+    // (3) binade estimates of this CTA's chunks (FP64 prefix of the chunk
+    //     sums), then their and their sub-chunks' increments for the three
+    //     candidate binades
+    double carry = 0.0;
+    for (int64_t s0 = 0; s0 < Cn; s0 += blockDim.x) {
+      const int64_t c = s0 + threadIdx.x;
+      const double v = (c < Cn) ? a.chunk_s[c] : 0.0;
+      const double incl = cv_block_scan_d(v, s_wd);
+      const double excl = carry + (incl - v);
+      if (c < Cn && (c % gridDim.x) == blockIdx.x)
+        a.chunk_e[c] = (int)(((unsigned long long)__double_as_longlong(excl) >> 52) & 0x7FF);
+      if ((int)threadIdx.x == (int)blockDim.x - 1) s_wd[0] = incl;  // the segment's total
+      __syncthreads();
+      carry += s_wd[0];
+      __syncthreads();
+    }
+    for (int64_t c = blockIdx.x; c < Cn; c += gridDim.x) {
+      const int64_t base = c * kSeqChunk;
+      const int len = (int)(lenh - base < kSeqChunk ? lenh - base : kSeqChunk);
+      seq_chunk_q_subs(a.terms, base, len, a.chunk_e[c], s_sub, a.sub_q + 3 * kSeqSubs * c,
+                       a.chunk_q + 3 * c);
+    }
+    if (!grid_sync(a.bar, nb, gen, a.status)) return false;
+    mark(kCvTraceQ);
+    // (4) CTA 0: one warp walks the chunks (staged in shared memory a segment
+    //     at a time) and replays, sub-chunk by sub-chunk, those it cannot pass
     if (blockIdx.x == 0) {
       long long* sQ = reinterpret_cast<long long*>(smem);
       int* sE = reinterpret_cast<int*>(sQ + 3 * kCvSeg);
-      double* sC = reinterpret_cast<double*>(sE + kCvSeg);            // a chunk's terms
-      long long* sS = reinterpret_cast<long long*>(sC + kSeqChunk);  // its sub-chunk windows
+      double* sT = reinterpret_cast<double*>(sE + kCvSeg);            // a chunk's terms
+      long long* sS = reinterpret_cast<long long*>(sT + kSeqChunk);  // its sub-chunk Q
       unsigned long long mb = s_m0;
-      double carry = 0.0;
       for (int64_t seg = 0; seg < Cn; seg += kCvSeg) {
         const int64_t segend = (seg + kCvSeg < Cn) ? seg + kCvSeg : Cn;
-        for (int64_t s0 = seg; s0 < segend; s0 += blockDim.x) {
-          const int64_t c = s0 + threadIdx.x;
-          const double v = (c < segend) ? a.chunk_s[c] : 0.0;
-          const double incl = cv_block_scan_d(v, s_wd);
-          if (c < segend) {
-            const double excl = carry + (incl - v);
-            const int eb = (int)(((unsigned long long)__double_as_longlong(excl) >> 52) & 0x7FF);
-            const int e0 = a.chunk_e[c];
-            sE[c - seg] = eb;
-#pragma unroll
-            for (int d = 0; d < 3; d++) {
-              const int k = eb - 1 + d - e0;
-              sQ[(c - seg) * 3 + d] =
-                  (k >= 0 && k < kSeqWin) ? a.chunk_q[(int64_t)kSeqWin * c + k] : -1;
-            }
-          }
-          if ((int)threadIdx.x == (int)blockDim.x - 1) s_wd[0] = incl;  // the segment's total
-          __syncthreads();
-          carry += s_wd[0];
-          __syncthreads();
-        }
+        for (int64_t i = threadIdx.x; i < (segend - seg) * 3; i += blockDim.x)
+          sQ[i] = a.chunk_q[seg * 3 + i];
+        for (int64_t i = threadIdx.x; i < segend - seg; i += blockDim.x) sE[i] = a.chunk_e[seg + i];
+        __syncthreads();
         if (threadIdx.x < 32) {
           int64_t c = (seg == 0) ? 1 : seg;  // chunk 0 was replayed with the terms
           while (c < segend) {
@@ -412,25 +399,11 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
             if (c >= segend) break;
             const int64_t base = c * kSeqChunk;
             const int len = (int)(lenh - base < kSeqChunk ? lenh - base : kSeqChunk);
-            // every load of the chunk in flight at once, then replay from
-            // shared memory
-            const long long* wsrc = a.sub_q + (int64_t)kSeqSubs * kSeqWin * c;
-            if (len == kSeqChunk) {
-              double r[kSeqChunk / 32];
-              long long q[kSeqSubs];
-#pragma unroll
-              for (int j = 0; j < kSeqChunk / 32; j++) r[j] = a.terms[base + j * 32 + threadIdx.x];
-#pragma unroll
-              for (int j = 0; j < kSeqSubs; j++) q[j] = wsrc[j * 32 + threadIdx.x];
-#pragma unroll
-              for (int j = 0; j < kSeqChunk / 32; j++) sC[j * 32 + threadIdx.x] = r[j];
-#pragma unroll
-              for (int j = 0; j < kSeqSubs; j++) sS[j * 32 + threadIdx.x] = q[j];
-            } else {
-              for (int k = threadIdx.x; k < len; k += 32) sC[k] = a.terms[base + k];
-            }
+            for (int k = threadIdx.x; k < len; k += 32) sT[k] = a.terms[base + k];
+            for (int k = threadIdx.x; k < 3 * kSeqSubs; k += 32)
+              sS[k] = a.sub_q[3 * kSeqSubs * c + k];
             __syncwarp();
-            seq_replay_chunk_warp(sC, len, sS, a.chunk_e[c], mb);
+            seq_replay_chunk_warp(sT, len, sS, sE[c - seg], mb);
             __syncwarp();
             c++;
           }

@@ -193,8 +193,8 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   const size_t b_zero = al(sizeof(CvFusedState)) + b_bar + 4 * b_rec + 4 * b_top;
   const size_t need = b_zero + 4 * b_rec + al(sizeof(double) * (size_t)lenh) +
                       al(sizeof(double) * (size_t)Cn) + al(sizeof(int) * (size_t)Cn) +
-                      al(sizeof(long long) * 32 * (size_t)Cn) +
-                      al(sizeof(long long) * 16 * 32 * (size_t)Cn);
+                      al(sizeof(long long) * 3 * (size_t)Cn) +
+                      al(sizeof(long long) * 48 * (size_t)Cn);
   char* base = static_cast<char*>(workspace(kSlotCvTerms, need));
   if (!base) return workspace_error();
   CvFusedArgs a{};
@@ -215,7 +215,7 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   a.chunk_e = reinterpret_cast<int*>(base + off);
   off += al(sizeof(int) * (size_t)Cn);
   a.chunk_q = reinterpret_cast<long long*>(base + off);
-  off += al(sizeof(long long) * 32 * (size_t)Cn);
+  off += al(sizeof(long long) * 3 * (size_t)Cn);
   a.sub_q = reinterpret_cast<long long*>(base + off);
   a.wcoef[0] = wec;
   a.wcoef[1] = woc;
@@ -243,19 +243,14 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   WC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return fail(WC_ERR_UNSUPPORTED, "device without cooperative launch");
   // Dynamic shared memory: the replay's staging (1024 chunks' candidate
-  // increments and binades, one chunk's terms and its sub-chunk windows),
+  // increments and binades, one chunk's terms and its sub-chunk increments),
   // the MODWT tiles or the DWT coarse levels (two buffers of kCvCoarseMax).
   size_t smem = (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) + 1024 * sizeof(double) +
-                16 * 32 * sizeof(long long);
+                48 * sizeof(long long);
   const size_t vsize = (c.prec == WC_F32) ? 4 : 8;
   if (c.ttype == 1) {
-    // Tiles small enough that both halves give every CTA (about three per
-    // SM) two or more of them, but at least 512 values (the halo rows grow
-    // with the fused levels).
-    int target = (c.prec == WC_F32) ? 4096 : 2048;
-    while (target > 512 && 2 * lenh / target < (int64_t)6 * sms) target >>= 1;
     size_t gs = 0;
-    WC_TRY(modwt_inv_groups(lenh, J1, c.F, c.prec, target, a.grp, &a.ngroups, &gs));
+    WC_TRY(modwt_inv_groups(lenh, J1, c.F, c.prec, 0, a.grp, &a.ngroups, &gs));
     smem = std::max(smem, gs);
   } else {
     int lc = 0;

@@ -36,9 +36,9 @@ struct CvFusedArgs {
   void* tmp[2][2];       // intermediate scaling sequences per half (T, lenh each)
   double* terms;         // lenh loss terms
   double* chunk_s;       // per chunk of kSeqChunk terms: FP64 sum (any order)
-  int* chunk_e;          // per chunk: e0, the lowest binade above all its terms
-  long long* chunk_q;    // per chunk: integer increments for the binades e0 .. e0+31
-  long long* sub_q;      // per chunk: the same for its 16 sub-chunks of 64 terms
+  int* chunk_e;          // binade estimate of the running sum at the chunk's start
+  long long* chunk_q;    // 3 per chunk: increments for the binades chunk_e - 1 .. + 1
+  long long* sub_q;      // 16 x 3 per chunk: the same for its 64-term sub-chunks
   CvFusedState* st;
   unsigned int* bar;     // grid barrier words (grid_bar_words, zero)
   unsigned int* status;  // status word (bit 0: a bounded wait gave up)
@@ -54,11 +54,11 @@ struct CvFusedArgs {
   // Optional phase timer (nullptr: off): CTA 0 adds the wall time (ns) of
   // each phase over the whole search, slots 0 .. kCvMaxGroups-1 for the
   // transform's level groups (DWT: 0 = the coarse CTA phase, 1 + k = fine
-  // level k), then the loss terms and the replay.
+  // level k), then the loss terms, the increments and the replay.
   unsigned long long* trace;
 };
-constexpr int kCvTraceTerms = kCvMaxGroups, kCvTraceReplay = kCvMaxGroups + 1,
-              kCvTraceSlots = kCvMaxGroups + 2;
+constexpr int kCvTraceTerms = kCvMaxGroups, kCvTraceQ = kCvMaxGroups + 1,
+              kCvTraceReplay = kCvMaxGroups + 2, kCvTraceSlots = kCvMaxGroups + 3;
 
 // Level groups of the time-ordered MODWT inverse of an n-sample signal with
 // J levels, coarsest first, as the tiled inverse runs them (tile target

@@ -59,18 +59,19 @@ static __device__ __noinline__ double dd_to_double_slow(float hi, float lo) {
 
 __device__ __forceinline__ dd dd_from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned int hw = (unsigned int)(b >> 32);
-  const int E = (int)((hw >> 20) & 0x7FF);  // biased FP64 exponent
-  // ef = E - 1023 + 127; lo's exponent ef - 23 must stay >= 1.
-  if (E < 1023 - 100 || E > 1023 + 127) return dd_from_double_slow(x);
-  const unsigned int sign = hw & 0x80000000u;
-  const unsigned int ef = (unsigned int)(E - 896);
-  const unsigned long long f = b & ((1ull << 52) - 1);
-  const float hi = __uint_as_float(sign | (ef << 23) | (unsigned int)(f >> 29));
-  const unsigned int rb = (unsigned int)((f >> 6) & 0x7FFFFF);  // next 23 bits
-  const float t = __uint_as_float(sign | ((ef - 23) << 23) | rb);
-  const float base = __uint_as_float(sign | ((ef - 23) << 23));
-  return {hi, __fsub_rn(t, base)};
+  const unsigned int lw = (unsigned int)b, hw = (unsigned int)(b >> 32);
+  const unsigned int E = (hw >> 20) & 0x7FF;  // biased FP64 exponent
+  // ef = E - 1023 + 127 must lie in [27, 254]: lo's exponent ef - 23 >= 1.
+  if (E - (1023u - 100u) > 227u) return dd_from_double_slow(x);
+  // Bits 29..60 of x hold the top 23 fraction bits and the low 9 exponent
+  // bits; subtracting 896 from that exponent field modulo 2^9 leaves ef
+  // (< 256, so bit 31 stays clear), and the sign goes into bit 31.
+  const unsigned int hib = (__funnelshift_r(lw, hw, 29) - (384u << 23)) | (hw & 0x80000000u);
+  // lo: the next 23 fraction bits (bits 6..28 of x) under exponent ef - 23,
+  // minus the implicit bit of that exponent.
+  const unsigned int baseb = (hib & 0xFF800000u) - (23u << 23);
+  const unsigned int rb = (lw >> 6) & 0x7FFFFFu;
+  return {__uint_as_float(hib), __fsub_rn(__uint_as_float(baseb | rb), __uint_as_float(baseb))};
 }
 
 // hi + lo as an FP64 value, assembled with integer operations: hi's 24-bit

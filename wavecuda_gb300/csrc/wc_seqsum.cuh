@@ -11,11 +11,13 @@
 // ties and a zero m take the serial rule (a real FP64 addition).
 //
 // Terms are grouped in chunks of kSeqChunk, each split into sub-chunks of
-// kSeqSub.  For every chunk and sub-chunk the integer increments Q are
-// computed in parallel for a window of kSeqWin binades starting just above
-// the chunk's largest term (-1 where a term ties).  One warp then walks the
-// chunks 32 at a time with a prefix sum of their Q (for the binade the
-// running sum is in); a chunk it cannot pass (binade crossing, tie, zero m)
+// kSeqSub.  The binade of the running sum at a chunk's start is that of the
+// FP64 prefix of the chunk sums or a neighbour (any summation order is far
+// closer than a factor of two), so the integer increments Q of every chunk
+// and sub-chunk are computed in parallel for those three binades (-1 where a
+// term ties).  One warp then walks the chunks 32 at a time with a prefix sum
+// of their Q (for the binade the running sum is in); a chunk it cannot pass
+// (binade crossing, tie, zero m)
 // is walked sub-chunk by sub-chunk, and only a sub-chunk with an event is
 // replayed term by term: a warp prefix sum of q finds the first term that
 // ties or leaves the binade, everything before it is added at once and that
@@ -31,7 +33,6 @@ namespace wc {
 constexpr int kSeqChunk = 1024;                // terms per chunk
 constexpr int kSeqSub = 64;                    // terms per sub-chunk
 constexpr int kSeqSubs = kSeqChunk / kSeqSub;  // sub-chunks per chunk (16)
-constexpr int kSeqWin = 32;                    // binades of the Q window
 constexpr uint64_t kSeqFrac = (1ull << 52) - 1;
 
 // q = rne(v / u) for the binade with biased exponent eb_m; bad when the term
@@ -62,42 +63,52 @@ __device__ __forceinline__ void seq_q_of(double v, int eb_m, long long& q, bool&
   q = (long long)((M >> s) + (rem > half ? 1 : 0));
 }
 
-// Q of a chunk's 16 sub-chunks for the window of binades e0 .. e0 + 31
-// (CTA-wide, blockDim 256; t: the chunk's terms in shared memory, len of
-// them).  Warp w covers sub-chunks 2w and 2w + 1, lane k the binade e0 + k:
-// each lane walks the sub-chunk's terms and sums its q (-1 when a term ties
-// or reaches the binade).  sub_out[s * 32 + k] for the 16 sub-chunks, then
-// the chunk's window chunk_out[k] = sum over its sub-chunks.  s_win: 16 x 32
-// long longs of shared scratch.
-__device__ __forceinline__ void seq_window_q(const double* t, int len, int e0, long long* s_win,
-                                             long long* sub_out, long long* chunk_out) {
+// Q of one chunk and of its 16 sub-chunks of 64 terms for the binades
+// eb0 - 1 .. eb0 + 1 (CTA-wide, blockDim 256: warp w covers sub-chunks 2w and
+// 2w + 1, two terms per lane each).  sub_out receives 16 x 3 values,
+// chunk_out 3 (-1 where a term ties or reaches the binade's size).
+__device__ __forceinline__ void seq_chunk_q_subs(const double* __restrict__ v, int64_t base,
+                                                 int len, int eb0, long long* s_sub /* 48 */,
+                                                 long long* sub_out, long long* chunk_out) {
   const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < 2; j++) {
     const int sb = 2 * w + j;
-    long long tot = 0;
-    bool bad = false;
-    const int k0 = sb * kSeqSub, k1 = min(len, k0 + kSeqSub);
-    for (int k = k0; k < k1; k++) {
-      long long q;
-      bool b;
-      seq_q_of(t[k], e0 + l, q, b);
-      tot += q;
-      bad |= b;
+    long long tot[3] = {0, 0, 0};
+    bool bad[3] = {false, false, false};
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int k = sb * kSeqSub + r * 32 + l;
+      if (k < len) {
+        const double x = v[base + k];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          long long q;
+          bool b;
+          seq_q_of(x, eb0 - 1 + d, q, b);
+          tot[d] += q;
+          bad[d] |= b;
+        }
+      }
     }
-    const long long r = (bad || k0 >= len) ? -1 : tot;
-    s_win[sb * kSeqWin + l] = (k0 >= len) ? 0 : r;
-    sub_out[sb * kSeqWin + l] = r;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      long long t = tot[d];
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      const bool anybad = __any_sync(0xffffffffu, bad[d]);
+      if (l == 0) s_sub[sb * 3 + d] = anybad ? -1 : t;
+    }
   }
   __syncthreads();
-  if (threadIdx.x < kSeqWin) {
-    long long t2 = 0;
+  if (threadIdx.x < kSeqSubs * 3) sub_out[threadIdx.x] = s_sub[threadIdx.x];
+  if (threadIdx.x < 3) {
+    long long t = 0;
     for (int sb = 0; sb < kSeqSubs; sb++) {
-      const long long q = s_win[sb * kSeqWin + threadIdx.x];
-      if (q < 0 || t2 < 0) t2 = -1;
-      else t2 += q;
+      const long long q = s_sub[sb * 3 + threadIdx.x];
+      if (q < 0 || t < 0) t = -1;
+      else t += q;
     }
-    chunk_out[threadIdx.x] = t2;
+    chunk_out[threadIdx.x] = t;
   }
   __syncthreads();
 }
@@ -142,18 +153,22 @@ __device__ __forceinline__ int64_t seq_walk(const long long* sQ, const int* sE, 
 }
 
 // One warp walks the sub-chunks sb .. 15 of one chunk while each one's Q
-// (win[s * kSeqWin + eb(m) - e0]) is valid and keeps m inside its binade;
-// returns the first sub-chunk not passed (16 when all were).
-__device__ __forceinline__ int seq_walk_subs(const long long* win, int e0, int sb,
+// (sub[3 s + d] for the binades eb0 - 1 + d) is valid for m's binade and
+// keeps m inside it; returns the first sub-chunk not passed (16 when all
+// were).  Same rule as seq_walk.
+__device__ __forceinline__ int seq_walk_subs(const long long* sub, int eb0, int sb,
                                              unsigned long long& mb) {
   const int l = threadIdx.x & 31;
   const int s = sb + l;
-  const int i = (int)(mb >> 52) - e0;
+  const int eb = (int)(mb >> 52);
   long long q = 0;
   bool ok = false;
-  if (s < kSeqSubs && mb != 0ull && i >= 0 && i < kSeqWin) {
-    q = win[s * kSeqWin + i];
-    ok = q >= 0;
+  if (s < kSeqSubs && mb != 0ull) {
+    const int i = eb - eb0 + 1;
+    if (i >= 0 && i <= 2) {
+      q = sub[3 * s + i];
+      ok = q >= 0;
+    }
   }
   const unsigned okm = __ballot_sync(0xffffffffu, ok);
   const int nok = (okm == 0xffffffffu) ? 32 : __ffs(~okm) - 1;
@@ -219,16 +234,15 @@ __device__ __forceinline__ void seq_replay_sub_warp(const double* __restrict__ v
 
 // One warp replays a whole chunk onto mb, sub-chunk by sub-chunk: a run of
 // sub-chunks whose Q applies is added at once, the others are replayed term
-// by term.  v: the chunk's terms (16-byte aligned), len of them; win: its
-// sub-chunk windows (16 x kSeqWin, binades from e0), or nullptr to replay
-// every sub-chunk.
+// by term.  v: the chunk's terms, len of them; sub: its 16 x 3 sub-chunk Q
+// (binades eb0 - 1 .. eb0 + 1), or nullptr to replay every sub-chunk.
 __device__ __forceinline__ void seq_replay_chunk_warp(const double* __restrict__ v, int len,
-                                                      const long long* win, int e0,
+                                                      const long long* sub, int eb0,
                                                       unsigned long long& mb) {
   const int nsub = (len + kSeqSub - 1) / kSeqSub;
   int sb = 0;
   while (sb < nsub) {
-    if (win && len == kSeqChunk) sb = seq_walk_subs(win, e0, sb, mb);
+    if (sub && len == kSeqChunk) sb = seq_walk_subs(sub, eb0, sb, mb);
     if (sb >= nsub) break;
     if ((sb + 1) * kSeqSub <= len) {
       seq_replay_sub_warp(v + sb * kSeqSub, mb);
