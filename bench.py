@@ -565,6 +565,8 @@ def batch_bench(wc, args):
         wc.check(L.wc_batch_autotune(plan, buf.ptr, C.byref(ms_tune)))
         grid = C.c_int()
         wc.check(L.wc_batch_plan_info(plan, C.byref(grid), None))
+        npairs = C.c_int()
+        wc.check(L.wc_batch_plan_pairs(plan, C.byref(npairs)))
         s = wc.default_stream()
         e0, e1 = wc.Event(), wc.Event()
         buf.upload(data, s)
@@ -616,6 +618,65 @@ def batch_bench(wc, args):
         r["algorithmic_bytes"] = tot
         r["aggregate_gbs"] = tot / (dev_ms / 1e3) / 1e9
         r["hbm_frac"] = r["aggregate_gbs"] / hbm
+        r["paired_searches"] = npairs.value
+        out[PREC[prec]] = r
+    out["skewed"] = skewed_batch_bench(wc)
+    return out
+
+
+def skewed_batch_bench(wc):
+    """A batch whose few long CV searches outlast the rest: 16 MODWT 2^20
+    signals (J = 10, four per filter) among 1024 DWT D4 2^12 signals, all CV
+    soft.  Device time with the plan's pairing (the longest searches split
+    over two CTAs) and with pairing off (WAVECUDA_BATCH_PAIRS=0), same
+    results."""
+    import ctypes as C
+    from wavecuda_gb300 import signals as sg
+    L = wc.lib()
+    specs = [(20, f, 1) for f in (1, 2, 3, 4) for _ in range(4)] + [(12, 2, 0)] * 1024
+    sigs, chunks, off = [], [], 0
+    shapes = list(sg.SHAPES)
+    for i, (k, filt, tt) in enumerate(specs):
+        n = 1 << k
+        J = min(10, wc.max_levels(n, filt))
+        chunks.append(sg.noisy(sg.SHAPES[shapes[i % len(shapes)]](n, i), 5.0, seed=9100 + i))
+        sigs.append(wc.Signal(off, n, J, tt, filt, 2, 1, 0, J - 1, 0.0, 1e-8))
+        off += n
+    data = np.concatenate(chunks)
+    out = {"workload": "16 MODWT CV signals n = 2^20 (J = 10, 4 per filter) + 1024 DWT D4 CV "
+                       "signals n = 2^12, soft, tol 1e-8", "samples": int(data.size)}
+    arr = (wc.Signal * len(sigs))(*sigs)
+    s = wc.default_stream()
+    for prec in (0, 1):
+        r = {}
+        ys = {}
+        for mode in ("paired", "unpaired"):
+            if mode == "unpaired":
+                os.environ["WAVECUDA_BATCH_PAIRS"] = "0"
+            plan = C.c_void_p()
+            try:
+                wc.check(L.wc_batch_plan_create(arr, len(sigs), prec, C.byref(plan)))
+            finally:
+                os.environ.pop("WAVECUDA_BATCH_PAIRS", None)
+            npairs = C.c_int()
+            wc.check(L.wc_batch_plan_pairs(plan, C.byref(npairs)))
+            buf = wc.DeviceBuffer(8 * data.size)
+            ms = []
+            for _ in range(2):  # the first run instantiates the graph
+                buf.upload(data, s)
+                e0, e1 = wc.Event(), wc.Event()
+                e0.record(s)
+                wc.check(L.wc_batch_run_device(plan, buf.ptr, s))
+                e1.record(s)
+                wc.check(L.wc_stream_synchronize(s))
+                ms.append(e0.elapsed_ms(e1))
+            ys[mode] = buf.download(np.float64, data.size, s)
+            wc.check(L.wc_batch_plan_destroy(plan))
+            buf.free()
+            r[mode + "_device_ms"] = ms[-1]
+            r[mode + "_pairs"] = npairs.value
+        r["speedup"] = r["unpaired_device_ms"] / r["paired_device_ms"]
+        r["max_abs_diff"] = float(np.max(np.abs(ys["paired"] - ys["unpaired"])))
         out[PREC[prec]] = r
     return out
 

@@ -211,11 +211,17 @@ typedef struct {
 typedef struct wc_batch_plan_s* wc_batch_plan;
 
 /* Validates the signals, orders the work queue largest-first, sizes the
- * per-CTA scratch and allocates the plan's device buffers. */
+ * per-CTA scratch and allocates the plan's device buffers.  When a few long
+ * CV searches would otherwise run on after the rest of the batch, the
+ * longest are each split over two CTAs (one half-signal inverse each per
+ * golden step, same results); the environment variable
+ * WAVECUDA_BATCH_PAIRS=0 turns this off. */
 WC_API int wc_batch_plan_create(const wc_signal* signals, int nsig, int precision,
                                 wc_batch_plan* plan);
 WC_API int wc_batch_plan_destroy(wc_batch_plan plan);
 WC_API int wc_batch_plan_info(wc_batch_plan plan, int* grid, size_t* scratch_bytes);
+/* Number of signals whose CV search the plan splits over two CTAs. */
+WC_API int wc_batch_plan_pairs(wc_batch_plan plan, int* npairs);
 /* Times a few grid sizes on a scratch copy of data (device) and keeps the
  * fastest; data is not modified.  Plans created later in the process (and
  * wc_smooth_batch) start from the grid found, for the same precision. */

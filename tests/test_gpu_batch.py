@@ -90,3 +90,45 @@ def test_batch_graph_replay_and_plan(gpu, oracle):
     assert ms.value > 0
     gpu.check(L.wc_batch_plan_destroy(plan))
     buf.free()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_paired_search(gpu, oracle, prec, tmp_path, monkeypatch):
+    """The CV searches too long for one CTA run on two (a leader and a
+    partner, one half-signal inverse each per golden step): exact FP64 gives
+    the same bits as the single-CTA search and as the oracle; double-float
+    stays within its tolerance of it."""
+    data, sigs = make_batch(gpu, oracle, 40, 6, 14, seed=6, kinds=(1, 2))
+    trace = tmp_path / "trace.csv"
+    monkeypatch.setenv("WAVECUDA_BATCH_TRACE", str(trace))
+    monkeypatch.setenv("WAVECUDA_BATCH_PAIRS", "1")
+    y2, r2 = gpu.smooth_batch(data, sigs, prec)
+    assert gpu.device_status() == 0
+    rows = [l.split(",") for l in trace.read_text().splitlines()[1:]]
+    roles = {(int(r[1]), int(r[2])) for r in rows}
+    paired = sorted(i for i, role in roles if role == 2)
+    assert paired and all((i, 1) in roles for i in paired)
+    assert all(sigs[i].threshtype == 2 for i in paired)
+    assert len(rows) == len(sigs) + len(paired)
+    monkeypatch.setenv("WAVECUDA_BATCH_PAIRS", "0")
+    y1, r1 = gpu.smooth_batch(data, sigs, prec)
+    for i, s in enumerate(sigs):
+        sl = slice(s.offset, s.offset + s.len)
+        if prec == 0:
+            assert r2[i].thresh == r1[i].thresh and r2[i].iterations == r1[i].iterations, i
+            assert (r2[i].kept, r2[i].zeroed) == (r1[i].kept, r1[i].zeroed), i
+            assert np.array_equal(y2[sl], y1[sl]), i
+        else:
+            # the loss partials add in another order: a near-tie late in the
+            # search may go the other way, moving the threshold within the
+            # search's final bracket
+            assert abs(r2[i].thresh - r1[i].thresh) <= 1e-4 * r1[i].thresh + 1e-12, i
+            scale = np.max(np.abs(y1[sl])) + 1e-300
+            assert np.max(np.abs(y2[sl] - y1[sl])) <= 1e-4 * scale, i
+    if prec == 0:
+        for i in paired:
+            s = sigs[i]
+            x = data[s.offset:s.offset + s.len]
+            yr, tr = oracle.smooth(x, s.nlevels, s.ttype, s.filter, s.threshtype, s.thresh,
+                                   s.hardness, s.minlevel, s.maxlevel, s.tol)
+            assert r2[i].thresh == tr and np.array_equal(y2[s.offset:s.offset + s.len], yr), i

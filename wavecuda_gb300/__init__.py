@@ -129,6 +129,7 @@ def lib() -> C.CDLL:
     L.wc_batch_plan_create.argtypes = [C.POINTER(Signal), C.c_int, C.c_int, C.POINTER(_vp)]
     L.wc_batch_plan_destroy.argtypes = [_vp]
     L.wc_batch_plan_info.argtypes = [_vp, _ip, C.POINTER(C.c_size_t)]
+    L.wc_batch_plan_pairs.argtypes = [_vp, _ip]
     L.wc_batch_autotune.argtypes = [_vp, _vp, C.POINTER(C.c_float)]
     L.wc_batch_run_device.argtypes = [_vp, _vp, _vp]
     L.wc_batch_results.argtypes = [_vp, C.POINTER(SignalResult), _vp]

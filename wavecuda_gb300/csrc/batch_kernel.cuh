@@ -28,6 +28,7 @@
 #include "wc_bulk.cuh"
 #include "wc_common.cuh"
 #include "wc_dd.cuh"
+#include "wc_grid.cuh"
 #include "wc_taps2.cuh"
 
 namespace wc {
@@ -715,10 +716,11 @@ __device__ double bseq_sum(const double* v, int64_t n, SumShared& sh) {
 
 // ------------------------------------------------------ CV loss (block) --
 
+// Terms j0 .. j1-1 of the loss.
 template <class Y>
-__device__ void bcv_terms(const Y* ye, const Y* yo, const double* xn, int64_t lenh,
-                          double* terms) {
-  for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
+__device__ void bcv_terms(const Y* ye, const Y* yo, const double* xn, int64_t lenh, int64_t j0,
+                          int64_t j1, double* terms) {
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     double yie, yio;
     if (j == 0) {
       yie = to_d(yo[0]);
@@ -764,9 +766,9 @@ __device__ __forceinline__ dd dd_sqr(dd a) {
   return r;
 }
 
-// Sum over the block of one double-float value per thread; the FP64 result
-// is valid in every thread.
-__device__ double bdd_reduce(dd v, SumShared& sh) {
+// Sum over the block of one double-float value per thread; the result is
+// valid in every thread.
+__device__ dd bdd_reduce(dd v, SumShared& sh) {
   for (int o = 16; o > 0; o >>= 1) {
     const dd w{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
     v = PDD::add(v, w);
@@ -784,9 +786,39 @@ __device__ double bdd_reduce(dd v, SumShared& sh) {
     sh.red_lo[0] = t.lo;
   }
   __syncthreads();
-  const double r = dd_to_double(dd{sh.red_hi[0], sh.red_lo[0]});
+  const dd r{sh.red_hi[0], sh.red_lo[0]};
   __syncthreads();
   return r;
+}
+
+// Double-float sum of the loss terms j0 .. j1-1, in block order (the
+// precisions other than exact FP64; the result is valid in every thread).
+template <class P>
+__device__ dd bcv_part(const typename P::V* ye, const typename P::V* yo, const double* xn,
+                       int64_t lenh, int64_t j0, int64_t j1, SumShared& sh) {
+  const dd half{0.5f, 0.f};
+  dd acc{0.f, 0.f};
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    dd yie, yio;
+    if (j == 0) {
+      yie = as_dd(yo[0]);
+      yio = PDD::add(as_dd(ye[0]), as_dd(ye[1]));
+      yio = dd{yio.hi * half.hi, yio.lo * half.hi};
+    } else if (j == lenh - 1) {
+      yio = as_dd(ye[lenh - 1]);
+      yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
+      yie = dd{yie.hi * half.hi, yie.lo * half.hi};
+    } else {
+      yio = PDD::add(as_dd(ye[j]), as_dd(ye[j + 1]));
+      yio = dd{yio.hi * half.hi, yio.lo * half.hi};
+      yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
+      yie = dd{yie.hi * half.hi, yie.lo * half.hi};
+    }
+    const dd a = PDD::sub(yie, dd_from_double(xn[2 * j]));
+    const dd b = PDD::sub(yio, dd_from_double(xn[2 * j + 1]));
+    acc = PDD::add(acc, PDD::add(dd_sqr(a), dd_sqr(b)));
+  }
+  return bdd_reduce(acc, sh);
 }
 
 // Sum of the interpolation loss terms (the quantity bcv_terms + bseq_sum
@@ -799,32 +831,10 @@ __device__ double bcv_sum(const typename P::V* ye, const typename P::V* yo, cons
                           int64_t lenh, double* terms, SumShared& sh) {
   using V = typename P::V;
   if constexpr (std::is_same<P, PExact>::value) {
-    bcv_terms<V>(ye, yo, xn, lenh, terms);
+    bcv_terms<V>(ye, yo, xn, lenh, 0, lenh, terms);
     return bseq_sum(terms, lenh, sh);
   } else {
-    const dd half{0.5f, 0.f};
-    dd acc{0.f, 0.f};
-    for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
-      dd yie, yio;
-      if (j == 0) {
-        yie = as_dd(yo[0]);
-        yio = PDD::add(as_dd(ye[0]), as_dd(ye[1]));
-        yio = dd{yio.hi * half.hi, yio.lo * half.hi};
-      } else if (j == lenh - 1) {
-        yio = as_dd(ye[lenh - 1]);
-        yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
-        yie = dd{yie.hi * half.hi, yie.lo * half.hi};
-      } else {
-        yio = PDD::add(as_dd(ye[j]), as_dd(ye[j + 1]));
-        yio = dd{yio.hi * half.hi, yio.lo * half.hi};
-        yie = PDD::add(as_dd(yo[j]), as_dd(yo[j - 1]));
-        yie = dd{yie.hi * half.hi, yie.lo * half.hi};
-      }
-      const dd a = PDD::sub(yie, dd_from_double(xn[2 * j]));
-      const dd b = PDD::sub(yio, dd_from_double(xn[2 * j + 1]));
-      acc = PDD::add(acc, PDD::add(dd_sqr(a), dd_sqr(b)));
-    }
-    return bdd_reduce(acc, sh);
+    return dd_to_double(bcv_part<P>(ye, yo, xn, lenh, 0, lenh, sh));
   }
 }
 
@@ -896,6 +906,184 @@ __device__ __forceinline__ bool range_ok(int64_t n, int J, int minl, int maxl, i
   return minl <= maxl && maxl < J;
 }
 
+// ------------------------------------------------------- paired CTAs --
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Longest wait at a pair barrier before it gives up.  The partner's first
+// wait spans the leader's forward transform and universal threshold of the
+// whole signal (a fraction of a second for 2^20 samples in one CTA).
+constexpr unsigned long long kPairWaitNs = 20ull * 1000000000ull;
+
+// Barrier of the two CTAs of a pair; nb counts the barriers this CTA has
+// passed.  Writes before it are visible to the other CTA after it (fence,
+// atomic arrival, acquire poll, fence).  Returns false in every thread when
+// the wait gave up (the status word then has its timeout bit).
+__device__ bool pair_sync(BatchPair* pr, unsigned int& nb, unsigned int* status) {
+  __syncthreads();
+  int ok = 1;
+  nb++;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(&pr->arrive, 1u);
+    const unsigned long long t0 = global_ns();
+    while (ld_acquire_gpu(&pr->arrive) < 2u * nb) {
+      if (global_ns() - t0 > kPairWaitNs) {
+        if (status) atomicOr(status, kStatusTimeout);
+        ok = 0;
+        break;
+      }
+      __nanosleep(128);
+    }
+    __threadfence();
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+// A signal's buffers in its (leader's) CTA scratch, in take order.  The
+// partner of a pair finds them by replaying the same takes on the leader's
+// scratch.
+template <class P>
+struct SigBufs {
+  typename P::T *xt, *w, *wsJ;
+  typename P::V *tA, *tB;
+  double* devbuf;
+  typename P::T *we, *weJ, *wo, *woJ;  // CV: coefficient stores of the halves
+  typename P::V* y[4];                 // CV: the four work vectors
+  double* terms;                       // CV: loss terms
+};
+
+template <class P>
+__device__ SigBufs<P> take_bufs(CtaScratch& cs, const BatchDesc& d) {
+  using T = typename P::T;
+  using V = typename P::V;
+  const int64_t n = d.n, lenh = n / 2;
+  const int J = d.J;
+  const bool mod = d.ttype == 1;
+  SigBufs<P> b{};
+  b.xt = cs.take<T>(n);
+  b.w = cs.take<T>(mod ? (int64_t)J * n : n);
+  b.wsJ = cs.take<T>(mod ? n : 1);
+  b.tA = cs.take<V>(n);
+  b.tB = cs.take<V>(n);
+  b.devbuf = cs.take<double>(mod ? (int64_t)J * n : n);
+  if (d.threshtype == 2) {
+    const int lv1 = J - 1;
+    b.we = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
+    b.weJ = cs.take<T>(mod ? lenh : 1);
+    b.wo = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
+    b.woJ = cs.take<T>(mod ? lenh : 1);
+    for (int k = 0; k < 4; k++) b.y[k] = cs.take<V>(lenh);
+    b.terms = cs.take<double>(lenh);
+  }
+  return b;
+}
+
+// Whether a CV signal searches at all (thresh.cpp:223-231 returns early).
+__device__ __forceinline__ bool cv_runs(const BatchDesc& d, int L) {
+  return range_ok(d.n, d.J, d.minl, d.maxl, L) && d.J > 1;
+}
+
+// The two-fold CV golden-section search (thresh.cpp:240-325) on the
+// forwarded halves in b: each step thresholds and inverts both halves for a
+// candidate and evaluates the interpolation loss.  role 0: one CTA does it
+// all.  role 1 / 2: the leader / partner of a pair invert the even / odd
+// half and compute the first / second half of the loss terms, meeting at
+// two barriers per step (after the inverses, after the terms); both reduce
+// the same values the same way, so they take the same branches.  tA, tB:
+// this CTA's level buffers; nb: pair barriers passed so far.  Returns false
+// when a pair barrier gave up.
+template <int F, class P>
+__device__ bool cv_search(const BatchDesc& d, int role, BatchPair* pr, unsigned int* status,
+                          unsigned int nb, const SigBufs<P>& b, typename P::V* tA,
+                          typename P::V* tB, const double* x, double t_univ, PipeShared& sh,
+                          double& t_out, int& iters_out, double& mm_out) {
+  using T = typename P::T;
+  using V = typename P::V;
+  const int64_t lenh = d.n / 2;
+  const int tt = d.ttype, L = filter_len(F), lv1 = d.J - 1, maxl1 = d.maxl - 1;
+  const bool half_ok = range_ok(lenh, lv1, d.minl, maxl1, L);
+  auto step = [&](int k, double tk) {
+    // threshold(we|wo, y_k, tk) then transform(y_k, BWD)
+    if (!half_ok) return;  // never thresholded: y_k stays zero
+    if ((role == 1 && (k & 1)) || (role == 2 && !(k & 1))) return;  // the other CTA's half
+    Th<P> th{to_v<P>(tk), d.hardness, d.minl, maxl1};
+    const bool even = (k & 1) == 0;
+    const T* ws = even ? b.we : b.wo;
+    const T* wJ = even ? b.weJ : b.woJ;
+    // DWT: coarse slots k*2^(J-1), k>0, come from y's previous content
+    inv_any<F, P, V>(tt, ws, wJ, (tt == 0) ? b.y[k] : nullptr, b.y[k], lenh, lv1, th, tA, tB);
+  };
+  bool ok = true;
+  auto loss = [&](int p) -> double {
+    const V* ye = b.y[2 * p];
+    const V* yo = b.y[2 * p + 1];
+    if (role == 0) return __dmul_rn(bcv_sum<P>(ye, yo, x, lenh, b.terms, sh.sum), 0.5);
+    ok = pair_sync(pr, nb, status);  // both halves inverted
+    if (!ok) return 0.0;
+    const int64_t mid = lenh / 2;
+    const int64_t j0 = (role == 1) ? 0 : mid, j1 = (role == 1) ? mid : lenh;
+    if constexpr (std::is_same<P, PExact>::value) {
+      bcv_terms<V>(ye, yo, x, lenh, j0, j1, b.terms);
+      ok = pair_sync(pr, nb, status);  // all terms written
+      if (!ok) return 0.0;
+      return __dmul_rn(bseq_sum(b.terms, lenh, sh.sum), 0.5);
+    } else {
+      const dd part = bcv_part<P>(ye, yo, x, lenh, j0, j1, sh.sum);
+      if (threadIdx.x == 0) {
+        pr->part[role - 1][0] = part.hi;
+        pr->part[role - 1][1] = part.lo;
+      }
+      ok = pair_sync(pr, nb, status);  // both partial sums written
+      if (!ok) return 0.0;
+      const dd tot = PDD::add(dd{pr->part[0][0], pr->part[0][1]}, dd{pr->part[1][0], pr->part[1][1]});
+      return __dmul_rn(dd_to_double(tot), 0.5);
+    }
+  };
+  const double R = 0.61803399, C = __dsub_rn(1.0, R);
+  double ta = 0., tc = t_univ;
+  double tb = __dmul_rn(tc, 0.5);
+  double t0 = ta, t2 = tb, t1 = __dsub_rn(tb, __dmul_rn(C, __dsub_rn(tb, ta))), t3 = tc;
+  double min_margin = 1e300;
+  int iters = 0;
+  step(0, t1);
+  step(1, t1);
+  step(2, t2);
+  step(3, t2);
+  double m1 = loss(0);
+  if (!ok) return false;
+  double m2 = loss(1);
+  if (!ok) return false;
+  while (fabs(__dsub_rn(t3, t0)) > __dmul_rn(d.tol, __dadd_rn(t1, t2))) {
+    if (iters > 50) break;
+    if (m1 != 0.0) min_margin = fmin(min_margin, fabs(__dsub_rn(m1, m2)) / fabs(m1));
+    if (m2 < m1) {
+      t0 = t1; t1 = t2; t2 = __dadd_rn(__dmul_rn(R, t2), __dmul_rn(C, t3));
+      m1 = m2;
+      step(2, t2);
+      step(3, t2);
+      m2 = loss(1);
+      if (!ok) return false;
+    } else {
+      t3 = t2; t2 = t1; t1 = __dadd_rn(__dmul_rn(R, t1), __dmul_rn(C, t0));
+      m2 = m1;
+      step(0, t1);
+      step(1, t1);
+      m1 = loss(0);
+      if (!ok) return false;
+    }
+    iters++;
+  }
+  t_out = m1 < m2 ? t1 : t2;
+  iters_out = iters;
+  mm_out = min_margin;
+  return true;
+}
+
 template <int F, class P>
 __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch cs, PipeShared& sh) {
   using T = typename P::T;
@@ -906,15 +1094,18 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
   const int64_t n = d.n, lenh = n / 2;
   const int J = d.J, tt = d.ttype, L = filter_len(F);
   const bool mod = (tt == 1);
+  BatchPair* pr = (d.pair > 0) ? a.pairs + (d.pair - 1) : nullptr;
+  if (pr && threadIdx.x == 0) atomicExch(&pr->leader, blockIdx.x + 1u);  // the partner's way in
 
+  const SigBufs<P> b = take_bufs<P>(cs, d);
+  T* xt = b.xt;
+  T* w = b.w;
+  T* wsJ = b.wsJ;
+  V* tA = b.tA;
+  V* tB = b.tB;
+  double* devbuf = b.devbuf;
   // x in the working precision
-  T* xt = cs.take<T>(n);
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) xt[i] = (T)x[i];
-  T* w = cs.take<T>(mod ? (int64_t)J * n : n);
-  T* wsJ = cs.take<T>(mod ? n : 1);
-  V* tA = cs.take<V>(n);
-  V* tB = cs.take<V>(n);
-  double* devbuf = cs.take<double>(mod ? (int64_t)J * n : n);
   __syncthreads();
 
   double t = d.thresh, t_univ = 0.0, min_margin = 1e300;
@@ -922,7 +1113,7 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
   fwd_any<F, P, T>(tt, xt, w, wsJ, n, J, tA, tB);
 
   if (d.threshtype == 2) {
-    if (!range_ok(n, J, d.minl, d.maxl, L) || J <= 1) {
+    if (!cv_runs(d, L)) {
       if (threadIdx.x == 0) {
         res->thresh = 0.0;
         res->iterations = 0;
@@ -931,83 +1122,49 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
         res->kept = res->zeroed = 0;
         res->min_margin = 0.0;
       }
-      return;  // thresh.cpp:223-231: x untouched
+      return;  // thresh.cpp:223-231: x untouched (never paired)
     }
     const int lv1 = J - 1;
-    const int maxl1 = d.maxl - 1;
     t_univ = buniv<T>(tt, w, n, J, d.minl, d.maxl, d.sq_nm1, d.sq_n, devbuf, sh);
-    // half-length vectors: coefficient stores and the four work vectors
-    T* we = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
-    T* weJ = cs.take<T>(mod ? lenh : 1);
-    T* wo = cs.take<T>(mod ? (int64_t)lv1 * lenh : lenh);
-    T* woJ = cs.take<T>(mod ? lenh : 1);
-    V* y[4];
-    for (int k = 0; k < 4; k++) y[k] = cs.take<V>(lenh);
-    double* terms = cs.take<double>(lenh);
     for (int64_t i = threadIdx.x; i < 4 * lenh; i += blockDim.x) {
       // zero the work vectors (fresh zero-filled pages in the reference)
-      (y[i / lenh])[i % lenh] = to_v<P>(0.0);
+      (b.y[i / lenh])[i % lenh] = to_v<P>(0.0);
     }
     for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) {
       reinterpret_cast<T*>(tA)[j] = (T)x[2 * j];
-      reinterpret_cast<T*>(tB)[j] = (T)x[2 * j + 1];
+      if (!pr) reinterpret_cast<T*>(tB)[j] = (T)x[2 * j + 1];
     }
     __syncthreads();
     // even/odd halves live in tA/tB's first halves as T; transform them
-    // with the upper halves of tA/tB as level buffers
+    // with the upper halves of tA/tB as level buffers (the partner of a
+    // pair forwards the odd half)
     {
       T* ev = reinterpret_cast<T*>(tA);
       T* od = reinterpret_cast<T*>(tB);
       V* uA = tA + lenh;
       V* uB = tB + lenh;
-      // forward of the even half uses uA/uB for levels; copy odd half first
-      // into devbuf so both fit.
-      T* od2 = reinterpret_cast<T*>(devbuf);
-      for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) od2[j] = od[j];
-      __syncthreads();
-      fwd_any<F, P, T>(tt, ev, we, weJ, lenh, lv1, uA, uB);
-      fwd_any<F, P, T>(tt, od2, wo, woJ, lenh, lv1, uA, uB);
-    }
-    const bool half_ok = range_ok(lenh, lv1, d.minl, maxl1, L);
-    auto step = [&](int k, double tk) {
-      // threshold(we|wo, y_k, tk) then transform(y_k, BWD)
-      if (!half_ok) return;  // never thresholded: y_k stays zero
-      Th<P> th{to_v<P>(tk), d.hardness, d.minl, maxl1};
-      const bool even = (k & 1) == 0;
-      const T* ws = even ? we : wo;
-      const T* wJ = even ? weJ : woJ;
-      // DWT: coarse slots k*2^(J-1), k>0, come from y's previous content
-      inv_any<F, P, V>(tt, ws, wJ, (tt == 0) ? y[k] : nullptr, y[k], lenh, lv1, th, tA, tB);
-    };
-    const double R = 0.61803399, C = __dsub_rn(1.0, R);
-    double ta = 0., tc = t_univ;
-    double tb = __dmul_rn(tc, 0.5);
-    double t0 = ta, t2 = tb, t1 = __dsub_rn(tb, __dmul_rn(C, __dsub_rn(tb, ta))), t3 = tc;
-    step(0, t1);
-    step(1, t1);
-    step(2, t2);
-    step(3, t2);
-    double m1 = __dmul_rn(bcv_sum<P>(y[0], y[1], x, lenh, terms, sh.sum), 0.5);
-    double m2 = __dmul_rn(bcv_sum<P>(y[2], y[3], x, lenh, terms, sh.sum), 0.5);
-    while (fabs(__dsub_rn(t3, t0)) > __dmul_rn(d.tol, __dadd_rn(t1, t2))) {
-      if (iters > 50) break;
-      if (m1 != 0.0) min_margin = fmin(min_margin, fabs(__dsub_rn(m1, m2)) / fabs(m1));
-      if (m2 < m1) {
-        t0 = t1; t1 = t2; t2 = __dadd_rn(__dmul_rn(R, t2), __dmul_rn(C, t3));
-        m1 = m2;
-        step(2, t2);
-        step(3, t2);
-        m2 = __dmul_rn(bcv_sum<P>(y[2], y[3], x, lenh, terms, sh.sum), 0.5);
-      } else {
-        t3 = t2; t2 = t1; t1 = __dadd_rn(__dmul_rn(R, t1), __dmul_rn(C, t0));
-        m2 = m1;
-        step(0, t1);
-        step(1, t1);
-        m1 = __dmul_rn(bcv_sum<P>(y[0], y[1], x, lenh, terms, sh.sum), 0.5);
+      fwd_any<F, P, T>(tt, ev, b.we, b.weJ, lenh, lv1, uA, uB);
+      if (!pr) {
+        // the odd half moves to devbuf so that uA/uB stay free for levels
+        T* od2 = reinterpret_cast<T*>(devbuf);
+        for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) od2[j] = od[j];
+        __syncthreads();
+        fwd_any<F, P, T>(tt, od2, b.wo, b.woJ, lenh, lv1, uA, uB);
       }
-      iters++;
     }
-    t = m1 < m2 ? t1 : t2;
+    bool ok = true;
+    unsigned int nb = 0;
+    if (pr) {
+      if (threadIdx.x == 0) pr->t_univ = t_univ;
+      ok = pair_sync(pr, nb, a.status);  // both halves forwarded, work vectors zeroed
+    }
+    if (ok)
+      ok = cv_search<F, P>(d, pr ? 1 : 0, pr, a.status, nb, b, tA, tB, x, t_univ, sh, t, iters,
+                           min_margin);
+    if (!ok) {
+      if (threadIdx.x == 0) res->status = 1;
+      return;  // a pair barrier gave up: x untouched
+    }
     t = __ddiv_rn(t, d.rescale);
   } else if (d.threshtype == 1) {
     t_univ = buniv<T>(tt, w, n, J, 0, 0, d.sq_nm1, d.sq_n, devbuf, sh);
@@ -1060,26 +1217,84 @@ __device__ __noinline__ void smooth_one(const BatchArgs& a, int idx, CtaScratch 
   }
 }
 
+// The partner's share of a paired signal's CV search: it forwards the odd
+// half into the leader's coefficient store, then runs the search with the
+// leader (cv_search, role 2) and leaves; the leader finishes the signal.
+template <int F, class P>
+__device__ __noinline__ void partner_one(const BatchArgs& a, int idx, CtaScratch cs,
+                                         PipeShared& sh) {
+  using T = typename P::T;
+  using V = typename P::V;
+  const BatchDesc d = a.desc[idx];
+  if (d.threshtype != 2 || d.pair <= 0 || !cv_runs(d, filter_len(F))) return;
+  BatchPair* pr = a.pairs + (d.pair - 1);
+  const double* x = a.data + d.off;
+  const int64_t n = d.n, lenh = n / 2;
+  __shared__ unsigned int s_leader;
+  if (threadIdx.x == 0) {
+    const unsigned long long t0 = global_ns();
+    unsigned int l;
+    while ((l = ld_acquire_gpu(&pr->leader)) == 0u) {
+      if (global_ns() - t0 > kPairWaitNs) {
+        if (a.status) atomicOr(a.status, kStatusTimeout);
+        break;
+      }
+      __nanosleep(128);
+    }
+    s_leader = l;
+  }
+  __syncthreads();
+  const unsigned int leader = s_leader;
+  __syncthreads();
+  if (leader == 0u) return;
+  CtaScratch lcs{a.scratch + (size_t)(leader - 1u) * a.scratch_per_cta, 0};
+  const SigBufs<P> b = take_bufs<P>(lcs, d);
+  T* od = cs.take<T>(lenh);
+  V* pA = cs.take<V>(n);
+  V* pB = cs.take<V>(n);
+  for (int64_t j = threadIdx.x; j < lenh; j += blockDim.x) od[j] = (T)x[2 * j + 1];
+  __syncthreads();
+  fwd_any<F, P, T>(d.ttype, od, b.wo, b.woJ, lenh, d.J - 1, pA, pB);
+  unsigned int nb = 0;
+  if (!pair_sync(pr, nb, a.status)) return;  // both halves forwarded
+  const double t_univ = pr->t_univ;
+  double t = 0.0, mm = 0.0;
+  int iters = 0;
+  cv_search<F, P>(d, 2, pr, a.status, nb, b, pA, pB, x, t_univ, sh, t, iters, mm);
+}
+
 template <class P>
 __global__ void __launch_bounds__(BT) smooth_batch_kernel(BatchArgs a) {
   __shared__ PipeShared sh;
-  __shared__ int s_sig;
+  __shared__ int s_unit;
   CtaScratch cs{a.scratch + (size_t)blockIdx.x * a.scratch_per_cta, 0};
   while (true) {
-    if (threadIdx.x == 0) s_sig = atomicAdd(a.counter, 1);
+    if (threadIdx.x == 0) s_unit = atomicAdd(a.counter, 1);
     __syncthreads();
-    const int k = s_sig;
+    const int k = s_unit;
     __syncthreads();
-    if (k >= a.nsig) break;
-    const int idx = a.order[k];
+    if (k >= a.nunits) break;
+    const unsigned long long t_start = (a.trace && threadIdx.x == 0) ? global_ns() : 0ull;
+    const int u = a.order[k];
+    const bool partner = u < 0;
+    const int idx = partner ? -u - 1 : u;
     cs.off = 0;
-    switch (a.desc[idx].F) {
-      case 1: smooth_one<1, P>(a, idx, cs, sh); break;
-      case 2: smooth_one<2, P>(a, idx, cs, sh); break;
-      case 3: smooth_one<3, P>(a, idx, cs, sh); break;
-      case 4: smooth_one<4, P>(a, idx, cs, sh); break;
+    switch (a.desc[idx].F * 2 + (partner ? 1 : 0)) {
+      case 2: smooth_one<1, P>(a, idx, cs, sh); break;
+      case 3: partner_one<1, P>(a, idx, cs, sh); break;
+      case 4: smooth_one<2, P>(a, idx, cs, sh); break;
+      case 5: partner_one<2, P>(a, idx, cs, sh); break;
+      case 6: smooth_one<3, P>(a, idx, cs, sh); break;
+      case 7: partner_one<3, P>(a, idx, cs, sh); break;
+      case 8: smooth_one<4, P>(a, idx, cs, sh); break;
+      case 9: partner_one<4, P>(a, idx, cs, sh); break;
     }
     __syncthreads();
+    if (a.trace && threadIdx.x == 0) {
+      a.trace[3 * (size_t)k] = t_start;
+      a.trace[3 * (size_t)k + 1] = global_ns();
+      a.trace[3 * (size_t)k + 2] = blockIdx.x;
+    }
   }
 }
 

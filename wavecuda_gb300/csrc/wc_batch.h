@@ -10,7 +10,9 @@ namespace wc {
 
 struct BatchDesc {
   int64_t off, n;           // signal = data[off .. off+n)
-  int J, ttype, F, threshtype, hardness, minl, maxl, pad;
+  int J, ttype, F, threshtype, hardness, minl, maxl;
+  int pair;                 // 0: one CTA; k > 0: its CV search is shared with a
+                            // second CTA through pairs[k - 1]
   double thresh, tol;       // manual threshold; CV tolerance
   double sq_n, sq_nm1;      // sqrt(2 log n), sqrt(2 log(n-1)) from the host libm
   double rescale;           // sqrt(1 - log 2 / log n)
@@ -22,15 +24,33 @@ struct BatchResult {
   long long kept, zeroed;
 };
 
+// Meeting point of the two CTAs that share a signal's CV search (zeroed
+// before every launch).  The leader runs the signal's pipeline in its own
+// scratch; the partner forwards the odd half, inverts the odd half at every
+// golden step and computes half of the loss terms.
+struct BatchPair {
+  unsigned int arrive;      // barrier arrivals of both CTAs
+  unsigned int leader;      // leader's CTA index + 1, published when it starts
+  unsigned int pad0[2];
+  double t_univ;            // the search's upper bound, from the leader
+  float part[2][2];         // double-float loss partials (hi, lo) of leader / partner
+  unsigned int pad1[22];
+};
+static_assert(sizeof(BatchPair) == 128, "one 128-byte line per pair");
+
 struct BatchArgs {
   const BatchDesc* desc;
   BatchResult* res;
-  const int* order;         // processing order (largest work first)
+  const int* order;         // queue units: i = signal i (its leader when paired),
+                            // -(i + 1) = the partner of paired signal i
   int* counter;             // work-queue head
-  int nsig;
+  int nunits;
   double* data;             // all signals, FP64, smoothed in place
   char* scratch;            // grid * scratch_per_cta bytes
   size_t scratch_per_cta;
+  BatchPair* pairs;         // one per paired signal
+  unsigned int* status;     // status word (bit 0: a bounded wait gave up)
+  unsigned long long* trace;  // nullptr, or per queue unit: start ns, end ns, CTA
 };
 
 size_t batch_scratch_bytes(const BatchDesc& d, int prec);
