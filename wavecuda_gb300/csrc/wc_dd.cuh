@@ -77,13 +77,12 @@ __device__ __forceinline__ dd dd_from_double(double x) {
 // hi + lo as an FP64 value, assembled with integer operations: hi's 24-bit
 // significand is placed at the top of a 53-bit one, lo's significand is
 // shifted into place and added or subtracted, and one normalising shift
-// fixes a carry or borrow (|lo| <= ulp(hi) for every pair this library
-// builds).  lo's bits below the 53-bit window are truncated, an error below
-// one FP64 ulp.
-__device__ __forceinline__ double dd_to_double(dd v) {
-  const unsigned int hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+// fixes a carry or borrow.  lo's bits below the 53-bit window are
+// truncated, an error below one FP64 ulp.  Any pair of finite floats.
+static __device__ __noinline__ double dd_to_double_gen(unsigned int hb, unsigned int lb) {
   const unsigned int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
-  if (eh == 0 || eh == 0xFF || el == 0xFF) return dd_to_double_slow(v.hi, v.lo);
+  if (eh == 0 || eh == 0xFF || el == 0xFF)
+    return dd_to_double_slow(__uint_as_float(hb), __uint_as_float(lb));
   unsigned long long A = (unsigned long long)((hb & 0x7FFFFFu) | 0x800000u) << 29;
   if (el != 0) {
     const unsigned long long ml = (lb & 0x7FFFFFu) | 0x800000u;
@@ -104,6 +103,29 @@ __device__ __forceinline__ double dd_to_double(dd v) {
   const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
                                   ((unsigned long long)e << 52) | (A & ((1ull << 52) - 1));
   return __longlong_as_double((long long)bits);
+}
+
+// The same value, branch-free for the pairs the arithmetic produces (hi
+// normal, lo zero, subnormal or at least 24 binades below hi, i.e. |lo| at
+// most about half an ulp of hi): double(hi) by moving its fields, then lo
+// counted in units of that double's ulp (truncated, as above) and added to
+// the 64-bit pattern.  Adding cannot carry out of the 29 low bits, which
+// double(hi) leaves zero; subtracting from a power-of-two hi borrows into
+// the binade below, whose ulp is half as large, so the count is doubled
+// there.  Bit-identical to dd_to_double_gen; other pairs go to it.
+__device__ __forceinline__ double dd_to_double(dd v) {
+  const unsigned int hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const unsigned int eh = (hb >> 23) & 0xFF, el = (lb >> 23) & 0xFF;
+  if (eh - 1u > 253u || el == 0xFFu || (el != 0u && eh < el + 24u)) return dd_to_double_gen(hb, lb);
+  const unsigned int hw = (hb & 0x80000000u) | (((hb & 0x7FFFFFFFu) >> 3) + (896u << 20));
+  const unsigned int lw = hb << 29;
+  const unsigned int ml = el ? ((lb & 0x7FFFFFu) | 0x800000u) : 0u;
+  const int sh = (int)eh - (int)el - 29;  // >= -5
+  unsigned int k = (sh <= 0) ? (ml << (-sh)) : (sh < 32 ? (ml >> sh) : 0u);
+  const bool neg = ((hb ^ lb) & 0x80000000u) != 0u;
+  if (neg && (hb & 0x7FFFFFu) == 0u) k <<= 1;
+  const unsigned long long b = ((unsigned long long)hw << 32) | lw;
+  return __longlong_as_double((long long)(neg ? b - k : b + k));
 }
 
 struct dd_acc {
