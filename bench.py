@@ -841,7 +841,8 @@ def reference(args):
 
 def profile_case(args):
     """Runs one small case twice (for ncu captures): forward then inverse of
-    a 2^log2n signal, DWT with J = min(16, log2n - 2) or MODWT with J = 4."""
+    a 2^log2n signal, DWT with J = min(16, log2n - 2) or MODWT with J = 4
+    (--profile-levels overrides J)."""
     import wavecuda_gb300 as wc
     n = 1 << args.log2n
     x = np.random.default_rng(0).standard_normal(n)
@@ -856,19 +857,20 @@ def profile_case(args):
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
     es = 4 if prec == 2 else 8
-    nb = n if kind == "dwt" else n * 2 * 4
+    Jm = args.profile_levels or 4
+    nb = n if kind == "dwt" else n * 2 * Jm
     a, b, r = wc.DeviceBuffer(es * n), wc.DeviceBuffer(es * nb), wc.DeviceBuffer(es * n)
     a.upload(x.astype(np.float32) if prec == 2 else x)
     if args.tiling:
         wc.set_dwt_tiling(filt, prec, *[int(v) for v in args.tiling.split(":")])
     for _ in range(2):
         if kind == "dwt":
-            J = min(16, args.log2n - 2)
+            J = args.profile_levels or min(16, args.log2n - 2)
             wc.check(L.wc_dwt_device(a.ptr, b.ptr, n, 1, J, filt, prec, None))
             wc.check(L.wc_dwt_device(b.ptr, r.ptr, n, 0, J, filt, prec, None))
         else:
-            wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 1, 4, filt, prec, None))
-            wc.check(L.wc_modwt_device(r.ptr, b.ptr, n, 0, 4, filt, prec, None))
+            wc.check(L.wc_modwt_device(a.ptr, b.ptr, n, 1, Jm, filt, prec, None))
+            wc.check(L.wc_modwt_device(r.ptr, b.ptr, n, 0, Jm, filt, prec, None))
         wc.check(L.wc_stream_synchronize(None))
     print("ok", args.profile_case)
 
@@ -880,6 +882,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--log2n", type=int, default=26)
+    ap.add_argument("--profile-levels", type=int, default=0)
     ap.add_argument("--filter", type=int, default=2)
     ap.add_argument("--levels", type=int, default=16)
     ap.add_argument("--precision", type=int, default=1)

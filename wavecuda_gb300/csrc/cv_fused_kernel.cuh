@@ -18,7 +18,8 @@
 //              half, then one grid-wide pass per finer level;
 //  2. the interpolation loss terms of interp_mse (thresh.cpp:344-385) and
 //     their per-chunk FP64 sums; CTA 0 also replays the first chunk, which
-//     depends on nothing else;
+//     depends on nothing else (exact FP64; the other precisions add the
+//     chunk sums in a fixed order in every CTA and stop here);
 //  3. per chunk, the binade of the running sum at its start (from the FP64
 //     prefix of the chunk sums) and the integer increments of the chunk and
 //     of its 64-term sub-chunks for the three candidate binades
@@ -303,10 +304,59 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
   };
 
   // ---- 2-4. loss of a pair of reconstructions ----------------------------
+  int evals = 0;  // loss evaluations so far (parity of the chunk-sum buffer)
   auto loss = [&](int pair, double& m) -> bool {
     const T* ye = static_cast<const T*>(a.rec[2 * pair]);
     const T* yo = static_cast<const T*>(a.rec[2 * pair + 1]);
     const int64_t Cn = (lenh + kSeqChunk - 1) / kSeqChunk;
+    if constexpr (!std::is_same<P, PExact>::value) {
+      // Double-float and FP32 reconstructions already differ from the
+      // reference's, so their loss needs no serial replay: FP64 chunk sums
+      // in a fixed order, then every CTA adds the chunk sums in the same
+      // fixed order and gets the same loss, with one barrier.  The two
+      // chunk-sum buffers alternate, so a CTA still reading the previous
+      // loss's sums never sees them overwritten.
+      double* cs = a.chunk_s + (int64_t)(evals & 1) * Cn;
+      evals++;
+      for (int64_t c = blockIdx.x; c < Cn; c += gridDim.x) {
+        const int64_t base = c * kSeqChunk;
+        const int len = (int)(lenh - base < kSeqChunk ? lenh - base : kSeqChunk);
+        double acc = 0.0;
+        for (int k = threadIdx.x; k < len; k += blockDim.x) acc += cv_term(ye, yo, a.x, lenh, base + k);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) s_wd[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double t = 0.0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_wd[w];
+          cs[c] = t;
+        }
+        __syncthreads();
+      }
+      if constexpr (TT == 0) {
+        // the coarse slots of this pair's reconstructions, for its next step
+        const int64_t ns = lenh >> J1;
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; it < 2 * ns; it += stride) {
+          const int h = it >= ns ? 1 : 0;
+          const int64_t k = it - h * ns;
+          static_cast<T*>(a.top[2 * pair + h])[k] =
+              static_cast<const T*>(a.rec[2 * pair + h])[k << J1];
+        }
+      }
+      if (!grid_sync(a.bar, nb, gen, a.status)) return false;
+      mark(kCvTraceTerms);
+      double acc = 0.0;
+      for (int64_t c = threadIdx.x; c < Cn; c += blockDim.x) acc += cs[c];
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+      if ((threadIdx.x & 31) == 0) s_wd[threadIdx.x >> 5] = acc;
+      __syncthreads();
+      double tot = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += s_wd[w];
+      __syncthreads();
+      m = __dmul_rn(tot, 0.5);
+      return true;
+    }
     // (2) the terms and per-chunk FP64 sums
     double* s_chunk0 = reinterpret_cast<double*>(smem);  // CTA 0: the first chunk's terms
     for (int64_t c = blockIdx.x; c < Cn; c += gridDim.x) {

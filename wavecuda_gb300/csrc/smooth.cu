@@ -192,7 +192,7 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   const size_t b_bar = 16384;  // barrier words (grid_bar_words), the phase timer in the last 1 KB
   const size_t b_zero = al(sizeof(CvFusedState)) + b_bar + 4 * b_rec + 4 * b_top;
   const size_t need = b_zero + 4 * b_rec + al(sizeof(double) * (size_t)lenh) +
-                      al(sizeof(double) * (size_t)Cn) + al(sizeof(int) * (size_t)Cn) +
+                      al(sizeof(double) * 2 * (size_t)Cn) + al(sizeof(int) * (size_t)Cn) +
                       al(sizeof(long long) * 3 * (size_t)Cn) +
                       al(sizeof(long long) * 48 * (size_t)Cn);
   char* base = static_cast<char*>(workspace(kSlotCvTerms, need));
@@ -211,7 +211,7 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   a.terms = reinterpret_cast<double*>(base + off);
   off += al(sizeof(double) * (size_t)lenh);
   a.chunk_s = reinterpret_cast<double*>(base + off);
-  off += al(sizeof(double) * (size_t)Cn);
+  off += al(sizeof(double) * 2 * (size_t)Cn);
   a.chunk_e = reinterpret_cast<int*>(base + off);
   off += al(sizeof(int) * (size_t)Cn);
   a.chunk_q = reinterpret_cast<long long*>(base + off);
@@ -242,11 +242,13 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   WC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   WC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return fail(WC_ERR_UNSUPPORTED, "device without cooperative launch");
-  // Dynamic shared memory: the replay's staging (1024 chunks' candidate
-  // increments and binades, one chunk's terms and its sub-chunk increments),
-  // the MODWT tiles or the DWT coarse levels (two buffers of kCvCoarseMax).
-  size_t smem = (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) + 1024 * sizeof(double) +
-                48 * sizeof(long long);
+  // Dynamic shared memory: the exact replay's staging (1024 chunks'
+  // candidate increments and binades, one chunk's terms and its sub-chunk
+  // increments), the MODWT tiles or the DWT coarse levels (two buffers of
+  // kCvCoarseMax).
+  size_t smem = (c.prec == WC_F64_EXACT) ? (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) +
+                                               1024 * sizeof(double) + 48 * sizeof(long long)
+                                         : 0;
   const size_t vsize = (c.prec == WC_F32) ? 4 : 8;
   if (c.ttype == 1) {
     size_t gs = 0;

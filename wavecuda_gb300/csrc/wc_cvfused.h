@@ -35,7 +35,8 @@ struct CvFusedArgs {
   void* top[4];          // DWT: previous reconstruction's coarse slots k 2^J1 (T, lenh >> J1)
   void* tmp[2][2];       // intermediate scaling sequences per half (T, lenh each)
   double* terms;         // lenh loss terms
-  double* chunk_s;       // per chunk of kSeqChunk terms: FP64 sum (any order)
+  double* chunk_s;       // per chunk of kSeqChunk terms: FP64 sum (any order); two
+                         // buffers of chunks (the non-exact losses alternate them)
   int* chunk_e;          // binade estimate of the running sum at the chunk's start
   long long* chunk_q;    // 3 per chunk: increments for the binades chunk_e - 1 .. + 1
   long long* sub_q;      // 16 x 3 per chunk: the same for its 64-term sub-chunks
