@@ -52,10 +52,8 @@ constexpr int kCvThreads = 256;
 constexpr int kCvSeg = 1024;  // chunks staged in shared memory by the replaying CTA
 
 // Dynamic shared memory the replay and the loss phase need (bytes): a
-// segment's candidate increments and binades, one chunk's terms and its
-// sub-chunk windows.
-constexpr size_t kCvSeqSmem = (size_t)kCvSeg * (3 * sizeof(long long) + sizeof(int)) +
-                              kSeqChunk * sizeof(double) + kSeqSubs * 3 * sizeof(long long);
+// segment's candidate increments and binades, or the first chunk's terms.
+constexpr size_t kCvSeqSmem = (size_t)kCvSeg * (3 * sizeof(long long) + sizeof(int));
 
 // thresh_coef (thresh.cpp:142-157) on an FP64 value, bit-identical to
 // `fabs(c) < t ? 0 : soft ? sign(c) * (fabs(c) - t) : c` with IEEE roundings:
@@ -430,11 +428,12 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
     mark(kCvTraceQ);
     // (4) CTA 0: one warp walks the chunks (staged in shared memory a segment
     //     at a time) and replays, sub-chunk by sub-chunk, those it cannot pass
+    //     (reading that chunk's sub-chunk increments and the terms of the
+    //     sub-chunks it replays straight from global memory: one round trip
+    //     each instead of staging the whole chunk)
     if (blockIdx.x == 0) {
       long long* sQ = reinterpret_cast<long long*>(smem);
       int* sE = reinterpret_cast<int*>(sQ + 3 * kCvSeg);
-      double* sT = reinterpret_cast<double*>(sE + kCvSeg);            // a chunk's terms
-      long long* sS = reinterpret_cast<long long*>(sT + kSeqChunk);  // its sub-chunk Q
       unsigned long long mb = s_m0;
       for (int64_t seg = 0; seg < Cn; seg += kCvSeg) {
         const int64_t segend = (seg + kCvSeg < Cn) ? seg + kCvSeg : Cn;
@@ -449,12 +448,8 @@ __global__ void __launch_bounds__(kCvThreads, 3) cv_fused_kernel(const CvFusedAr
             if (c >= segend) break;
             const int64_t base = c * kSeqChunk;
             const int len = (int)(lenh - base < kSeqChunk ? lenh - base : kSeqChunk);
-            for (int k = threadIdx.x; k < len; k += 32) sT[k] = a.terms[base + k];
-            for (int k = threadIdx.x; k < 3 * kSeqSubs; k += 32)
-              sS[k] = a.sub_q[3 * kSeqSubs * c + k];
-            __syncwarp();
-            seq_replay_chunk_warp(sT, len, sS, sE[c - seg], mb);
-            __syncwarp();
+            seq_replay_chunk_warp<SeqLdGlobal>(a.terms + base, len, a.sub_q + 3 * kSeqSubs * c,
+                                               sE[c - seg], mb);
             c++;
           }
         }

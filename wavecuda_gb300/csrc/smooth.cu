@@ -243,12 +243,9 @@ int cv_search_fused(const Ctx<T>& c, const T* wec, const T* woc, const double* x
   WC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) return fail(WC_ERR_UNSUPPORTED, "device without cooperative launch");
   // Dynamic shared memory: the exact replay's staging (1024 chunks'
-  // candidate increments and binades, one chunk's terms and its sub-chunk
-  // increments), the MODWT tiles or the DWT coarse levels (two buffers of
-  // kCvCoarseMax).
-  size_t smem = (c.prec == WC_F64_EXACT) ? (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) +
-                                               1024 * sizeof(double) + 48 * sizeof(long long)
-                                         : 0;
+  // candidate increments and binades; the first chunk's terms fit in it),
+  // the MODWT tiles or the DWT coarse levels (two buffers of kCvCoarseMax).
+  size_t smem = (c.prec == WC_F64_EXACT) ? (size_t)1024 * (3 * sizeof(long long) + sizeof(int)) : 0;
   const size_t vsize = (c.prec == WC_F32) ? 4 : 8;
   if (c.ttype == 1) {
     size_t gs = 0;

@@ -156,8 +156,26 @@ __device__ __forceinline__ int64_t seq_walk(const long long* sQ, const int* sE, 
 // (sub[3 s + d] for the binades eb0 - 1 + d) is valid for m's binade and
 // keeps m inside it; returns the first sub-chunk not passed (16 when all
 // were).  Same rule as seq_walk.
+// Loads of the replay helpers: from shared memory, or from global memory
+// that other CTAs wrote earlier in the same launch (ld.global.cg: served by
+// L2, never by a stale L1 or read-only-cache line).
+struct SeqLdShared {
+  template <class X>
+  __device__ __forceinline__ X operator()(const X* p) const {
+    return *p;
+  }
+};
+struct SeqLdGlobal {
+  template <class X>
+  __device__ __forceinline__ X operator()(const X* p) const {
+    return __ldcg(p);
+  }
+};
+
+template <class Ld = SeqLdShared>
 __device__ __forceinline__ int seq_walk_subs(const long long* sub, int eb0, int sb,
                                              unsigned long long& mb) {
+  const Ld ld{};
   const int l = threadIdx.x & 31;
   const int s = sb + l;
   const int eb = (int)(mb >> 52);
@@ -166,7 +184,7 @@ __device__ __forceinline__ int seq_walk_subs(const long long* sub, int eb0, int 
   if (s < kSeqSubs && mb != 0ull) {
     const int i = eb - eb0 + 1;
     if (i >= 0 && i <= 2) {
-      q = sub[3 * s + i];
+      q = ld(sub + 3 * s + i);
       ok = q >= 0;
     }
   }
@@ -192,10 +210,10 @@ __device__ __forceinline__ int seq_walk_subs(const long long* sub, int eb0, int 
 // term that ties or leaves the binade, everything before it is added at
 // once, that term with a real FP64 addition, and the rest continues.
 // v is 16-byte aligned.
-__device__ __forceinline__ void seq_replay_sub_warp(const double* __restrict__ v,
-                                                    unsigned long long& mb) {
+template <class Ld = SeqLdShared>
+__device__ __forceinline__ void seq_replay_sub_warp(const double* v, unsigned long long& mb) {
   const int l = threadIdx.x & 31;
-  const double2 pr = reinterpret_cast<const double2*>(v)[l];
+  const double2 pr = Ld{}(reinterpret_cast<const double2*>(v) + l);
   const double v0 = pr.x, v1 = pr.y;
   int pos = 0;
   while (pos < kSeqSub) {
@@ -235,22 +253,26 @@ __device__ __forceinline__ void seq_replay_sub_warp(const double* __restrict__ v
 // One warp replays a whole chunk onto mb, sub-chunk by sub-chunk: a run of
 // sub-chunks whose Q applies is added at once, the others are replayed term
 // by term.  v: the chunk's terms, len of them; sub: its 16 x 3 sub-chunk Q
-// (binades eb0 - 1 .. eb0 + 1), or nullptr to replay every sub-chunk.
-__device__ __forceinline__ void seq_replay_chunk_warp(const double* __restrict__ v, int len,
+// (binades eb0 - 1 .. eb0 + 1), or nullptr to replay every sub-chunk.  Ld:
+// SeqLdShared when v and sub are in shared memory, SeqLdGlobal when they are
+// global memory written earlier in the launch.
+template <class Ld = SeqLdShared>
+__device__ __forceinline__ void seq_replay_chunk_warp(const double* v, int len,
                                                       const long long* sub, int eb0,
                                                       unsigned long long& mb) {
+  const Ld ld{};
   const int nsub = (len + kSeqSub - 1) / kSeqSub;
   int sb = 0;
   while (sb < nsub) {
-    if (sub && len == kSeqChunk) sb = seq_walk_subs(sub, eb0, sb, mb);
+    if (sub && len == kSeqChunk) sb = seq_walk_subs<Ld>(sub, eb0, sb, mb);
     if (sb >= nsub) break;
     if ((sb + 1) * kSeqSub <= len) {
-      seq_replay_sub_warp(v + sb * kSeqSub, mb);
+      seq_replay_sub_warp<Ld>(v + sb * kSeqSub, mb);
     } else {
       // ragged tail: one term at a time (the same in every lane)
       for (int k = sb * kSeqSub; k < len; k++)
         mb = (unsigned long long)__double_as_longlong(
-            __dadd_rn(__longlong_as_double((long long)mb), v[k]));
+            __dadd_rn(__longlong_as_double((long long)mb), ld(v + k)));
     }
     sb++;
   }
