@@ -207,6 +207,28 @@ int check_levels(int64_t n, int nlevels, int filterlen) {
   return nlevels;
 }
 
+// Tuning signal: x[i] uniform in [-1, 1) from a 64-bit integer hash of i
+// (splitmix64 finaliser), so that transforms see the mix of magnitudes and
+// signs of real data rather than a constant (whose zero details would not
+// time like real ones).
+template <class T>
+__global__ void fill_noise_kernel(T* x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long z = (unsigned long long)i + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[i] = (T)((double)(z >> 11) * (1.0 / 4503599627370496.0) - 1.0);
+  }
+}
+
+int fill_noise(void* x, int64_t n, size_t es, cudaStream_t s) {
+  if (es == 4) fill_noise_kernel<float><<<1024, 256, 0, s>>>(static_cast<float*>(x), n);
+  else fill_noise_kernel<double><<<1024, 256, 0, s>>>(static_cast<double*>(x), n);
+  return after_launch("fill_noise_kernel");
+}
+
 unsigned int* existing_status_word() {
   std::lock_guard<std::mutex> lk(g_mu);
   int d = 0;

@@ -1282,8 +1282,11 @@ extern "C" int wc_tune_dwt(int filter, int precision, int log2n, float* best_ms)
     return fail(WC_ERR_NOMEM, "tuning buffers");
   }
   cudaStream_t s = lib_stream();
-  // any finite data will do: small integers written as bytes
-  cudaMemsetAsync(a, 0x3c, es * (size_t)n, s);
+  if (fill_noise(a, n, es, s) != WC_OK) {
+    cudaFree(a);
+    cudaFree(b);
+    return fail(WC_ERR_CUDA, "tuning signal");
+  }
   const TileCfg keep = get_cfg(filter, precision);
   const int gm = gmax_of(filter);
   std::vector<TileCfg> cand;

@@ -383,7 +383,11 @@ extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, 
     return fail(WC_ERR_NOMEM, "tuning buffers");
   }
   cudaStream_t s = lib_stream();
-  cudaMemsetAsync(x, 0x3c, es * (size_t)n, s);
+  if (fill_noise(x, n, es, s) != WC_OK) {
+    cudaFree(x);
+    cudaFree(xm);
+    return fail(WC_ERR_CUDA, "tuning signal");
+  }
   const ModCfg keep = get_mod_cfg(filter, precision);
   const int base = (precision == WC_F32) ? 2048 : 1024;
   std::vector<std::pair<int, int>> cand;

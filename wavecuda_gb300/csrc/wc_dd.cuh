@@ -62,7 +62,12 @@ __device__ __forceinline__ dd dd_from_double(double x) {
   const unsigned int lw = (unsigned int)b, hw = (unsigned int)(b >> 32);
   const unsigned int E = (hw >> 20) & 0x7FF;  // biased FP64 exponent
   // ef = E - 1023 + 127 must lie in [27, 254]: lo's exponent ef - 23 >= 1.
-  if (E - (1023u - 100u) > 227u) return dd_from_double_slow(x);
+  // Zeros (common after thresholding) stay inline, as the generic path
+  // converts them: (+0, +0).
+  if (E - (1023u - 100u) > 227u) {
+    if ((b << 1) == 0ull) return {0.f, 0.f};
+    return dd_from_double_slow(x);
+  }
   // Bits 29..60 of x hold the top 23 fraction bits and the low 9 exponent
   // bits; subtracting 896 from that exponent field modulo 2^9 leaves ef
   // (< 256, so bit 31 stays clear), and the sign goes into bit 31.

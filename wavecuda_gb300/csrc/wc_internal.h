@@ -98,6 +98,10 @@ int noalloc_status_word(unsigned int** w);
 
 // The library's own non-blocking stream on the current device.
 cudaStream_t lib_stream();
+
+// Writes n pseudo-random values in [-1, 1) (FP64 for es == 8, FP32 for
+// es == 4) on stream s: the autotuners' test signal.
+int fill_noise(void* x, int64_t n, size_t es, cudaStream_t s);
 // Makes sure a CUDA device is usable and current.
 int ensure_device();
 
