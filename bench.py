@@ -293,7 +293,8 @@ def ours(args):
                 mt, fms, ims = wc.tune_modwt(f, p, args.log2n, 12)
                 tiling[f"MODWT {FILTERS[f]}/{PREC[p]}"] = {
                     "fwd_target": mt[0], "fwd_smem_kb": mt[1], "inv_target": mt[2],
-                    "inv_smem_kb": mt[3], "fwd_ms": round(fms, 4), "inv_ms": round(ims, 4)}
+                    "inv_smem_kb": mt[3], "inv_levels": wc.get_modwt_inv_levels(f, p),
+                    "fwd_ms": round(fms, 4), "inv_ms": round(ims, 4)}
 
     clocks = ClockSampler()
     clocks.start()

@@ -291,6 +291,12 @@ WC_API int wc_get_modwt_tiling(int filter, int precision, int* fwd_target, int* 
                                int* inv_target, int* inv_smem_kb);
 WC_API int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, float* fwd_ms,
                          float* inv_ms);
+/* Levels the inverse MODWT fuses per launch (2 or 3; 0 restores the
+ * filter's default: 3 for Haar, 2 otherwise).  More levels per launch move
+ * the intermediate scaling sequence through HBM fewer times but stage a
+ * deeper halo; wc_tune_modwt chooses it along with the tiling. */
+WC_API int wc_set_modwt_inv_levels(int filter, int precision, int levels);
+WC_API int wc_get_modwt_inv_levels(int filter, int precision, int* levels);
 
 /* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
  * BWD reads only s_J and d_1..d_J. */

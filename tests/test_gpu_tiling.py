@@ -77,16 +77,23 @@ def test_modwt_tilings_match_oracle(gpu, oracle, filt):
     x = np.random.default_rng(filt).standard_normal(n)
     ref = oracle.modwt_fwd(x, J, filt)
     keep = gpu.get_modwt_tiling(filt, 0)
+    keep_ni = gpu.get_modwt_inv_levels(filt, 0)
+    inv_ref = oracle.modwt_inv(ref, n, J, filt)
     try:
         for target, kb in ((256, 16), (1024, 48), (4096, 96), (16384, 200)):
             gpu.set_modwt_tiling(filt, 0, target, kb, target, kb)
             xm = gpu.transform(x, J, gpu.MODWT, filt, gpu.FWD, gpu.F64_EXACT)
             assert np.array_equal(xm, ref), (target, kb)
-            r = gpu.transform(xm, J, gpu.MODWT, filt, gpu.BWD, gpu.F64_EXACT, xmod=xm)
-            assert np.array_equal(r, oracle.modwt_inv(ref, n, J, filt)), (target, kb)
+            for ni in (2, 3):
+                gpu.set_modwt_inv_levels(filt, 0, ni)
+                r = gpu.transform(xm, J, gpu.MODWT, filt, gpu.BWD, gpu.F64_EXACT, xmod=xm)
+                assert np.array_equal(r, inv_ref), (target, kb, ni)
         with pytest.raises(gpu.WaveCudaError):
             gpu.set_modwt_tiling(filt, 0, 1000, 48, 1024, 48)
+        with pytest.raises(gpu.WaveCudaError):
+            gpu.set_modwt_inv_levels(filt, 0, 4)
         (t, f, i) = gpu.tune_modwt(filt, 1, 16, 8)
-        assert t[0] >= 256 and f > 0 and i > 0
+        assert t[0] >= 256 and f > 0 and i > 0 and gpu.get_modwt_inv_levels(filt, 1) in (2, 3)
     finally:
         gpu.set_modwt_tiling(filt, 0, *keep)
+        gpu.set_modwt_inv_levels(filt, 0, keep_ni)

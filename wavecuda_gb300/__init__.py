@@ -141,6 +141,8 @@ def lib() -> C.CDLL:
     L.wc_tune_dwt.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
     L.wc_set_modwt_tiling.argtypes = [C.c_int] * 6
     L.wc_get_modwt_tiling.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+    L.wc_set_modwt_inv_levels.argtypes = [C.c_int, C.c_int, C.c_int]
+    L.wc_get_modwt_inv_levels.argtypes = [C.c_int, C.c_int, _ip]
     L.wc_tune_modwt.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float),
                                 C.POINTER(C.c_float)]
     L.wc_device_count.argtypes = [_ip]
@@ -716,6 +718,17 @@ def get_modwt_tiling(filt, precision):
     v = [C.c_int() for _ in range(4)]
     check(lib().wc_get_modwt_tiling(filt, precision, *[C.byref(x) for x in v]))
     return tuple(x.value for x in v)
+
+
+def set_modwt_inv_levels(filt, precision, levels):
+    """Levels fused per inverse MODWT launch (2 or 3; 0 = the default)."""
+    check(lib().wc_set_modwt_inv_levels(filt, precision, levels))
+
+
+def get_modwt_inv_levels(filt, precision) -> int:
+    v = C.c_int()
+    check(lib().wc_get_modwt_inv_levels(filt, precision, C.byref(v)))
+    return v.value
 
 
 def tune_modwt(filt, precision, log2n=24, nlevels=12):

@@ -123,6 +123,7 @@ struct Geo {
 // the fastest measured candidates.
 struct ModCfg {
   int fwd_target, fwd_smem_kb, inv_target, inv_smem_kb;
+  int inv_levels;  // levels fused per inverse launch (2 or 3; 0: the filter's default)
 };
 
 std::mutex g_mcfg_mu;
@@ -131,7 +132,7 @@ bool g_mcfg_set[5][3] = {};
 
 ModCfg default_mod_cfg(int prec) {
   const int t = (prec == WC_F32) ? 4096 : 2048;
-  return ModCfg{t, 96, t, 96};
+  return ModCfg{t, 96, t, 96, 0};
 }
 
 ModCfg get_mod_cfg(int F, int prec) {
@@ -174,7 +175,10 @@ Geo<P> tile_geo(int64_t n, int l0, int halo, int arrays, int lead_rows, int targ
 }
 
 constexpr int nf_max(int F) { return 2; }
-constexpr int ni_max(int F) { return F == 1 ? 3 : 2; }
+// Levels fused per inverse launch: more levels mean fewer round trips of the
+// intermediate scaling sequence through HBM but a deeper halo
+// ((L-1)(2^NI - 1) rows); the tuner picks 2 or 3 per filter and precision.
+int ni_of(int F, const ModCfg& c) { return c.inv_levels ? c.inv_levels : (F == 1 ? 3 : 2); }
 
 template <int F, class P, int NF>
 int launch_fwd(const typename P::T* X, typename P::T* xmod, int64_t n, int l0, cudaStream_t s) {
@@ -235,8 +239,9 @@ int run_modwt(void* vx, void* vxmod, int64_t n, int sense, int J, cudaStream_t s
     }
     return WC_OK;
   }
+  const int nim = ni_of(F, get_mod_cfg(F, prec_of<P>()));
   T* tmp[2] = {nullptr, nullptr};
-  if (J > ni_max(F)) {
+  if (J > nim) {
     tmp[0] = static_cast<T*>(workspace(kSlotModwt0, sizeof(T) * (size_t)n));
     tmp[1] = static_cast<T*>(workspace(kSlotModwt1, sizeof(T) * (size_t)n));
     if (!tmp[0] || !tmp[1]) return workspace_error();
@@ -244,7 +249,7 @@ int run_modwt(void* vx, void* vxmod, int64_t n, int sense, int J, cudaStream_t s
   const T* Stop = xmod + (int64_t)2 * (J - 1) * n;
   int g = 0;
   for (int hi = J - 1; hi >= 0; g++) {
-    const int ni = std::min(ni_max(F), hi + 1);
+    const int ni = std::min(nim, hi + 1);
     const int l0 = hi - ni + 1;
     T* out = (l0 == 0) ? x : tmp[g & 1];
     if (ni == 3) WC_TRY((launch_inv<F, P, 3>(Stop, xmod, out, n, l0, s)));
@@ -339,9 +344,32 @@ extern "C" int wc_set_modwt_tiling(int filter, int precision, int fwd_target, in
                                    int inv_target, int inv_smem_kb) {
   using namespace wc;
   clear_error();
-  const ModCfg c{fwd_target, fwd_smem_kb, inv_target, inv_smem_kb};
+  ModCfg c{fwd_target, fwd_smem_kb, inv_target, inv_smem_kb, 0};
   WC_TRY(check_mod_cfg(filter, precision, c));
+  c.inv_levels = get_mod_cfg(filter, precision).inv_levels;
   set_mod_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_set_modwt_inv_levels(int filter, int precision, int levels) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  if (levels != 0 && levels != 2 && levels != 3)
+    return fail(WC_ERR_ARG, "inverse levels per launch must be 2, 3 or 0 (default)");
+  ModCfg c = get_mod_cfg(filter, precision);
+  c.inv_levels = levels;
+  set_mod_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_get_modwt_inv_levels(int filter, int precision, int* levels) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2 || !levels)
+    return fail(WC_ERR_ARG, "bad filter/precision/output");
+  *levels = ni_of(filter, get_mod_cfg(filter, precision));
   return WC_OK;
 }
 
@@ -360,8 +388,9 @@ extern "C" int wc_get_modwt_tiling(int filter, int precision, int* fwd_target, i
 }
 
 // Times the forward and the inverse MODWT (nlevels levels) of a 2^log2n
-// signal for each candidate tile target and shared-memory budget, and keeps
-// the fastest of each direction.
+// signal for each candidate tile target and shared-memory budget (and, for
+// the inverse, 2 or 3 levels per launch), and keeps the fastest of each
+// direction.
 extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, float* fwd_ms,
                              float* inv_ms) {
   using namespace wc;
@@ -401,34 +430,38 @@ extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, 
   ModCfg best = keep;
   int rc = WC_OK;
   for (const auto& c : cand) {
-    set_mod_cfg(filter, precision, ModCfg{c.first, c.second, c.first, c.second});
-    float mf = 1e30f, mi = 1e30f;
-    for (int rep = 0; rep < 3 && rc == WC_OK; rep++) {
-      cudaEventRecord(e0, s);
-      rc = modwt(x, xm, n, 1, J, filter, precision, s);
-      cudaEventRecord(e1, s);
-      if (rc == WC_OK) rc = modwt(x, xm, n, 0, J, filter, precision, s);
-      cudaEventRecord(e2, s);
-      cudaEventSynchronize(e2);
-      float a = 0.f, b = 0.f;
-      cudaEventElapsedTime(&a, e0, e1);
-      cudaEventElapsedTime(&b, e1, e2);
-      if (rep > 0) {
-        mf = std::min(mf, a);
-        mi = std::min(mi, b);
+    for (int ni : {2, 3}) {
+      set_mod_cfg(filter, precision, ModCfg{c.first, c.second, c.first, c.second, ni});
+      float mf = 1e30f, mi = 1e30f;
+      for (int rep = 0; rep < 3 && rc == WC_OK; rep++) {
+        cudaEventRecord(e0, s);
+        rc = modwt(x, xm, n, 1, J, filter, precision, s);
+        cudaEventRecord(e1, s);
+        if (rc == WC_OK) rc = modwt(x, xm, n, 0, J, filter, precision, s);
+        cudaEventRecord(e2, s);
+        cudaEventSynchronize(e2);
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, e0, e1);
+        cudaEventElapsedTime(&b, e1, e2);
+        if (rep > 0) {
+          mf = std::min(mf, a);
+          mi = std::min(mi, b);
+        }
+      }
+      if (rc != WC_OK) break;
+      if (ni == 2 && mf < bf) {  // the forward does not depend on ni
+        bf = mf;
+        best.fwd_target = c.first;
+        best.fwd_smem_kb = c.second;
+      }
+      if (mi < bi) {
+        bi = mi;
+        best.inv_target = c.first;
+        best.inv_smem_kb = c.second;
+        best.inv_levels = ni;
       }
     }
     if (rc != WC_OK) break;
-    if (mf < bf) {
-      bf = mf;
-      best.fwd_target = c.first;
-      best.fwd_smem_kb = c.second;
-    }
-    if (mi < bi) {
-      bi = mi;
-      best.inv_target = c.first;
-      best.inv_smem_kb = c.second;
-    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
