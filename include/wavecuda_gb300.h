@@ -297,6 +297,17 @@ WC_API int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, floa
  * deeper halo; wc_tune_modwt chooses it along with the tiling. */
 WC_API int wc_set_modwt_inv_levels(int filter, int precision, int levels);
 WC_API int wc_get_modwt_inv_levels(int filter, int precision, int* levels);
+/* Levels the forward MODWT fuses per launch on the 16-byte tiles (1, 2 or 3;
+ * 0 restores the default, 2; launches that fall back to the one-value tiles
+ * fuse at most 2).  wc_tune_modwt chooses it along with the tiling. */
+WC_API int wc_set_modwt_fwd_levels(int filter, int precision, int levels);
+WC_API int wc_get_modwt_fwd_levels(int filter, int precision, int* levels);
+/* 1 (the default): MODWT level kernels whose tiles allow it (one column, or
+ * a multiple of 16 bytes of columns, and 16-byte aligned buffers) stage,
+ * load and store 16 bytes per instruction; 0: every launch uses the
+ * one-value-per-instruction tiles.  Both give bit-identical results.  No
+ * counterpart in the reference. */
+WC_API int wc_set_modwt_vector(int enable);
 
 /* Time-ordered MODWT.  FWD: x (len) -> xmod (2*len*J).  BWD: xmod -> x.
  * BWD reads only s_J and d_1..d_J. */

@@ -112,6 +112,8 @@ class Oracle:
     def modwt_fwd(self, x, nlevels, filt):
         x = np.ascontiguousarray(x, dtype=np.float64)
         J = self.levels(x.size, nlevels, filt)
+        if J == 0:
+            raise ValueError(f"{nlevels} levels invalid for length {x.size}")
         xmod = np.zeros(2 * J * x.size)
         if self.lib.wo_modwt(_ptr(x), _ptr(xmod), x.size, FWD, J, filt):
             raise ValueError("oracle modwt rejected the arguments")
@@ -120,6 +122,8 @@ class Oracle:
     def modwt_po_fwd(self, x, nlevels, filt):
         x = np.ascontiguousarray(x, dtype=np.float64)
         J = self.levels(x.size, nlevels, filt)
+        if J == 0:
+            raise ValueError(f"{nlevels} levels invalid for length {x.size}")
         xmod = np.zeros(2 * J * x.size)
         if self.lib.wo_modwt_po(_ptr(x), _ptr(xmod), x.size, FWD, J, filt):
             raise ValueError("oracle modwt_po rejected the arguments")
@@ -227,6 +231,8 @@ class Reference:
     def modwt_fwd(self, x, nlevels, filt):
         x = np.array(x, dtype=np.float64, copy=True)
         J = self.levels(x.size, nlevels, filt)
+        if J == 0:
+            raise ValueError(f"{nlevels} levels invalid for length {x.size}")
         xmod = np.zeros(2 * J * x.size)
         r = self.lib.wref_transform(_ptr(x), _ptr(xmod), x.size, FWD, J, MODWT, filt,
                                     FILTER_LEN[filt])
@@ -246,6 +252,8 @@ class Reference:
     def modwt_po_fwd(self, x, nlevels, filt):
         x = np.array(x, dtype=np.float64, copy=True)
         J = self.levels(x.size, nlevels, filt)
+        if J == 0:
+            raise ValueError(f"{nlevels} levels invalid for length {x.size}")
         xmod = np.zeros(2 * J * x.size)
         if self.lib.wref_transform(_ptr(x), _ptr(xmod), x.size, FWD, J, MODWT_PO, filt,
                                    FILTER_LEN[filt]):

@@ -731,6 +731,23 @@ def get_modwt_inv_levels(filt, precision) -> int:
     return v.value
 
 
+def set_modwt_fwd_levels(filt, precision, levels):
+    """Levels fused per forward MODWT launch (1..3; 0 = the default, 2)."""
+    check(lib().wc_set_modwt_fwd_levels(filt, precision, levels))
+
+
+def get_modwt_fwd_levels(filt, precision) -> int:
+    v = C.c_int()
+    check(lib().wc_get_modwt_fwd_levels(filt, precision, C.byref(v)))
+    return v.value
+
+
+def set_modwt_vector(enable: bool) -> None:
+    """16-byte MODWT tiles where they apply (the default), or the
+    one-value-per-instruction tiles everywhere; both give the same bits."""
+    check(lib().wc_set_modwt_vector(1 if enable else 0))
+
+
 def tune_modwt(filt, precision, log2n=24, nlevels=12):
     """Autotunes the MODWT tiling; returns (tiling, fwd_ms, inv_ms)."""
     f, i = C.c_float(), C.c_float()

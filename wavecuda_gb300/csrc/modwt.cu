@@ -24,6 +24,7 @@
 // output is computed with the reference's term order, so WC_F64_EXACT stays
 // bit-identical however the levels are grouped.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 #include <vector>
@@ -33,6 +34,7 @@
 #include "wc_dd.cuh"
 #include "wc_taps2.cuh"
 #include "wc_modwt_math.cuh"
+#include "wc_modwt_vec.cuh"
 #include "wc_cvfused.h"
 
 namespace wc {
@@ -124,6 +126,7 @@ struct Geo {
 struct ModCfg {
   int fwd_target, fwd_smem_kb, inv_target, inv_smem_kb;
   int inv_levels;  // levels fused per inverse launch (2 or 3; 0: the filter's default)
+  int fwd_levels;  // levels fused per forward launch of the 16-byte tiles (1..3; 0: 2)
 };
 
 std::mutex g_mcfg_mu;
@@ -132,7 +135,7 @@ bool g_mcfg_set[5][3] = {};
 
 ModCfg default_mod_cfg(int prec) {
   const int t = (prec == WC_F32) ? 4096 : 2048;
-  return ModCfg{t, 96, t, 96, 0};
+  return ModCfg{t, 96, t, 96, 0, 0};
 }
 
 ModCfg get_mod_cfg(int F, int prec) {
@@ -180,6 +183,40 @@ constexpr int nf_max(int F) { return 2; }
 // ((L-1)(2^NI - 1) rows); the tuner picks 2 or 3 per filter and precision.
 int ni_of(int F, const ModCfg& c) { return c.inv_levels ? c.inv_levels : (F == 1 ? 3 : 2); }
 
+// Vectorised tiles (wc_modwt_vec.cuh) where they apply; wc_set_modwt_vector(0)
+// keeps every launch on the scalar tiles.
+std::atomic<int> g_modwt_vec{1};
+
+bool aligned16_host(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+// The 16-byte forward tiles: 1..3 fused levels (wc_modwt_vec.cuh).  Returns
+// WC_ERR_UNSUPPORTED when they do not apply to this launch.
+template <int F, class P, int NF>
+int launch_fwd_vec(const typename P::T* X, typename P::T* xmod, int64_t n, int l0, cudaStream_t s) {
+  constexpr int L = filter_len(F);
+  constexpr int W = mvec_w<P>();
+  if (!g_modwt_vec.load() || !aligned16_host(X) || !aligned16_host(xmod) || n % W != 0)
+    return WC_ERR_UNSUPPORTED;
+  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+  const size_t budget = (size_t)mc.fwd_smem_kb * 1024;
+  const int64_t d0 = (int64_t)1 << l0, nrows = n >> l0;
+  const int C = (int)std::min<int64_t>(d0, 32);
+  int M = (int)std::min<int64_t>(nrows, std::max(1, mc.fwd_target / C));
+  auto bytes = [&](int m) { return sizeof(typename P::T) * (size_t)mvec_fwd_values(L, NF, m, C, W); };
+  while (M > W && bytes(M) > budget) M >>= 1;
+  if (!mvec_ok(C, M, W)) return WC_ERR_UNSUPPORTED;
+  const size_t smem = bytes(M);
+  if (smem > 200 * 1024) return WC_ERR_UNSUPPORTED;
+  auto kern = modwt_fwd_vec<F, P, NF>;
+  WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t blocks = (d0 / C) * (nrows / M);
+  {
+    LaunchTimer lt("modwt_fwd_vec", s);
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(X, xmod, n, l0, C, M);
+  }
+  return after_launch("modwt_fwd_vec");
+}
+
 template <int F, class P, int NF>
 int launch_fwd(const typename P::T* X, typename P::T* xmod, int64_t n, int l0, cudaStream_t s) {
   constexpr int L = filter_len(F);
@@ -210,9 +247,27 @@ int launch_inv(const typename P::T* Stop, const typename P::T* xmod, typename P:
                int64_t n, int l0, cudaStream_t s) {
   constexpr int L = filter_len(F);
   constexpr int HR = (L - 1) * ((1 << NI) - 1);
+  constexpr int W = mvec_w<P>();
+  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+  if (g_modwt_vec.load() && aligned16_host(Stop) && aligned16_host(xmod) && aligned16_host(out) &&
+      n % W == 0) {
+    const int C = (int)std::min<int64_t>((int64_t)1 << l0, 32);
+    const int HRp = mvec_inv_halo(L, NI, C, W);
+    const Geo<P> g = tile_geo<P>(n, l0, HRp, mvec_inv_arrays(NI), 0, mc.inv_target,
+                                 (size_t)mc.inv_smem_kb * 1024);
+    if (mvec_ok(g.C, g.M, W)) {
+      auto kern = modwt_inv_vec<F, P, NI>;
+      WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
+      const int64_t blocks = (((int64_t)1 << l0) / g.C) * ((n >> l0) / g.M);
+      {
+        LaunchTimer lt("modwt_inv_vec", s);
+        kern<<<(unsigned)blocks, kThreads, g.smem, s>>>(Stop, xmod, out, n, l0, g.C, g.M, HRp);
+      }
+      return after_launch("modwt_inv_vec");
+    }
+  }
   // Stop tile, NI detail tiles and NI - 1 intermediates.
   const int arrays = 2 * NI;
-  const ModCfg mc = get_mod_cfg(F, prec_of<P>());
   Geo<P> g = tile_geo<P>(n, l0, HR, arrays, 0, mc.inv_target, (size_t)mc.inv_smem_kb * 1024);
   auto kern = modwt_inv_tiled<F, P, NI>;
   WC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem));
@@ -230,11 +285,19 @@ int run_modwt(void* vx, void* vxmod, int64_t n, int sense, int J, cudaStream_t s
   T* x = static_cast<T*>(vx);
   T* xmod = static_cast<T*>(vxmod);
   if (sense == 1) {
+    const ModCfg mc = get_mod_cfg(F, prec_of<P>());
+    const int nfv = mc.fwd_levels ? mc.fwd_levels : 2;
     for (int l = 0; l < J;) {
       const T* X = (l == 0) ? x : xmod + (int64_t)2 * (l - 1) * n;
-      const int nf = std::min(nf_max(F), J - l);
-      if (nf == 2) WC_TRY((launch_fwd<F, P, 2>(X, xmod, n, l, s)));
-      else WC_TRY((launch_fwd<F, P, 1>(X, xmod, n, l, s)));
+      int nf = std::min(nfv, J - l);
+      int r = nf == 3   ? launch_fwd_vec<F, P, 3>(X, xmod, n, l, s)
+              : nf == 2 ? launch_fwd_vec<F, P, 2>(X, xmod, n, l, s)
+                        : launch_fwd_vec<F, P, 1>(X, xmod, n, l, s);
+      if (r == WC_ERR_UNSUPPORTED) {
+        nf = std::min(nf_max(F), J - l);
+        r = nf == 2 ? launch_fwd<F, P, 2>(X, xmod, n, l, s) : launch_fwd<F, P, 1>(X, xmod, n, l, s);
+      }
+      WC_TRY(r);
       l += nf;
     }
     return WC_OK;
@@ -344,9 +407,10 @@ extern "C" int wc_set_modwt_tiling(int filter, int precision, int fwd_target, in
                                    int inv_target, int inv_smem_kb) {
   using namespace wc;
   clear_error();
-  ModCfg c{fwd_target, fwd_smem_kb, inv_target, inv_smem_kb, 0};
+  ModCfg c{fwd_target, fwd_smem_kb, inv_target, inv_smem_kb, 0, 0};
   WC_TRY(check_mod_cfg(filter, precision, c));
   c.inv_levels = get_mod_cfg(filter, precision).inv_levels;
+  c.fwd_levels = get_mod_cfg(filter, precision).fwd_levels;
   set_mod_cfg(filter, precision, c);
   return WC_OK;
 }
@@ -361,6 +425,35 @@ extern "C" int wc_set_modwt_inv_levels(int filter, int precision, int levels) {
   ModCfg c = get_mod_cfg(filter, precision);
   c.inv_levels = levels;
   set_mod_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_set_modwt_fwd_levels(int filter, int precision, int levels) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2)
+    return fail(WC_ERR_ARG, "bad filter/precision");
+  if (levels < 0 || levels > 3)
+    return fail(WC_ERR_ARG, "forward levels per launch must be 1, 2, 3 or 0 (default)");
+  ModCfg c = get_mod_cfg(filter, precision);
+  c.fwd_levels = levels;
+  set_mod_cfg(filter, precision, c);
+  return WC_OK;
+}
+
+extern "C" int wc_get_modwt_fwd_levels(int filter, int precision, int* levels) {
+  using namespace wc;
+  clear_error();
+  if (filter < 1 || filter > 4 || precision < 0 || precision > 2 || !levels)
+    return fail(WC_ERR_ARG, "bad filter/precision/output");
+  const int v = get_mod_cfg(filter, precision).fwd_levels;
+  *levels = v ? v : 2;
+  return WC_OK;
+}
+
+extern "C" int wc_set_modwt_vector(int enable) {
+  wc::clear_error();
+  wc::g_modwt_vec.store(enable ? 1 : 0);
   return WC_OK;
 }
 
@@ -422,50 +515,63 @@ extern "C" int wc_tune_modwt(int filter, int precision, int log2n, int nlevels, 
   std::vector<std::pair<int, int>> cand;
   for (int t : {base, 2 * base, 4 * base})
     for (int kb : {48, 72, 96}) cand.push_back({t, kb});
-  cudaEvent_t e0, e1, e2;
+  cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  cudaEventCreate(&e2);
   float bf = 1e30f, bi = 1e30f;
   ModCfg best = keep;
   int rc = WC_OK;
+  // Best of reps 2..3 of one direction under configuration c.
+  auto time_dir = [&](const ModCfg& c, int sense, float* ms) {
+    set_mod_cfg(filter, precision, c);
+    float m = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, s);
+      const int r = modwt(x, xm, n, sense, J, filter, precision, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      if (r != WC_OK) return r;
+      float a = 0.f;
+      cudaEventElapsedTime(&a, e0, e1);
+      if (rep > 0) m = std::min(m, a);
+    }
+    *ms = m;
+    return WC_OK;
+  };
+  // The forward first (the inverse reads its output), per tiling and levels
+  // per launch; then the inverse.
   for (const auto& c : cand) {
-    for (int ni : {2, 3}) {
-      set_mod_cfg(filter, precision, ModCfg{c.first, c.second, c.first, c.second, ni});
-      float mf = 1e30f, mi = 1e30f;
-      for (int rep = 0; rep < 3 && rc == WC_OK; rep++) {
-        cudaEventRecord(e0, s);
-        rc = modwt(x, xm, n, 1, J, filter, precision, s);
-        cudaEventRecord(e1, s);
-        if (rc == WC_OK) rc = modwt(x, xm, n, 0, J, filter, precision, s);
-        cudaEventRecord(e2, s);
-        cudaEventSynchronize(e2);
-        float a = 0.f, b = 0.f;
-        cudaEventElapsedTime(&a, e0, e1);
-        cudaEventElapsedTime(&b, e1, e2);
-        if (rep > 0) {
-          mf = std::min(mf, a);
-          mi = std::min(mi, b);
-        }
-      }
+    for (int nf : {1, 2, 3}) {
+      float m = 0.f;
+      rc = time_dir(ModCfg{c.first, c.second, keep.inv_target, keep.inv_smem_kb, keep.inv_levels, nf},
+                    1, &m);
       if (rc != WC_OK) break;
-      if (ni == 2 && mf < bf) {  // the forward does not depend on ni
-        bf = mf;
+      if (m < bf) {
+        bf = m;
         best.fwd_target = c.first;
         best.fwd_smem_kb = c.second;
+        best.fwd_levels = nf;
       }
-      if (mi < bi) {
-        bi = mi;
+    }
+    if (rc != WC_OK) break;
+  }
+  for (const auto& c : cand) {
+    if (rc != WC_OK) break;
+    for (int ni : {2, 3}) {
+      float m = 0.f;
+      rc = time_dir(ModCfg{best.fwd_target, best.fwd_smem_kb, c.first, c.second, ni,
+                           best.fwd_levels}, 0, &m);
+      if (rc != WC_OK) break;
+      if (m < bi) {
+        bi = m;
         best.inv_target = c.first;
         best.inv_smem_kb = c.second;
         best.inv_levels = ni;
       }
     }
-    if (rc != WC_OK) break;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
   cudaFree(x);
   cudaFree(xm);
   set_mod_cfg(filter, precision, rc == WC_OK ? best : keep);
