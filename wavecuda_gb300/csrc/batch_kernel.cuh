@@ -367,6 +367,68 @@ __device__ void bfwd_level_tiled(const S* src, int64_t N, int l, Emit&& emit) {
   }
 }
 
+// One FP32 forward level by the 16-byte tiles of wc_modwt_vec.cuh,
+// double-buffered like bfwd_level_tiled: a thread computes W = 4 adjacent
+// outputs of a row (4 rows of a single-column tile) with the operations of
+// bfwd_level_tiled per value, and emit(i, s, d) receives the outputs i ..
+// i+3 (consecutive in memory).  Returns false without doing anything when
+// the tiles do not apply (other precisions, too few rows, a source not
+// 16-byte aligned).
+template <int F, class P, class S, class EmitG>
+__device__ bool bfwd_level_vec(const S* src, int64_t N, int l, EmitG&& emit) {
+  if constexpr (!std::is_same<P, PF32>::value || !std::is_same<S, float>::value) {
+    return false;
+  } else {
+    constexpr int L = filter_len(F);
+    constexpr int W = 4;
+    constexpr int KT = mod_tile<float>();
+    const int64_t d0 = (int64_t)1 << l, rows = N >> l;
+    const int C = (int)(d0 < 32 ? d0 : 32);
+    int64_t M = rows;
+    auto rows_in = [&](int64_t m) { return (int64_t)mvec_fwd_rows(L, 1, 0, (int)m, C, W); };
+    while (M > W && rows_in(M) * C > KT) M >>= 1;
+    if (!mvec_ok(C, (int)M, W) || rows_in(M) * C > KT || ((uintptr_t)src & 15)) return false;
+    extern __shared__ __align__(16) unsigned char mod_smem[];
+    float* buf = reinterpret_cast<float*>(mod_smem);  // [stage][KT]
+    const int cs = __ffs(C) - 1;
+    const int64_t nb = d0 / C, ntiles = nb * (rows / M);
+    const int totc = (int)(rows_in(M) * C / W);
+    auto issue = [&](int64_t tile, int stage) {
+      float* Vs = buf + stage * KT;
+      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+      for (int j = threadIdx.x; j < totc; j += blockDim.x) {
+        const int e = j * W;
+        const int row = e >> cs, c = e & (C - 1);
+        cp_async16(Vs + e, src + (r0 + c) + ((m0 + row) & (rows - 1)) * d0);
+      }
+      cp_async_commit();
+    };
+    issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+      const int stage = (int)(tile & 1);
+      if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
+      else cp_async_commit();  // empty group keeps the wait count uniform
+      cp_async_wait_prior_1();
+      __syncthreads();
+      const float* Vs = buf + stage * KT;
+      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+      auto group = [&](auto rdc) {
+        constexpr int RD = decltype(rdc)::value;
+        for (int e = (int)threadIdx.x * W; e < (int)(M * C); e += (int)blockDim.x * W) {
+          const int row = e >> cs, c = e & (C - 1);
+          float sv[W], dv[W];
+          fwd_group<F, P, RD>(Vs, e, C, sv, dv);
+          emit((r0 + c) + (m0 + row) * d0, sv, dv);
+        }
+      };
+      if (C == 1) group(std::integral_constant<int, 1>{});
+      else group(std::integral_constant<int, 0>{});
+      __syncthreads();  // this stage is refilled two tiles later
+    }
+    return true;
+  }
+}
+
 template <int F, class P, class S>
 __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, int64_t N, int J,
                            typename P::V* tA, typename P::V* tB) {
@@ -379,6 +441,18 @@ __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, in
       if (l == J - 1) sJ[i] = P::st(s);
       else dst[i] = s;
     };
+    if constexpr (std::is_same<P, PF32>::value) {
+      // 16-byte stores of four outputs (scratch slices are 256-byte aligned)
+      auto emitg = [&](int64_t i, const float (&s)[4], const float (&d)[4]) {
+        *reinterpret_cast<float4*>(dd_out + i) = make_float4(d[0], d[1], d[2], d[3]);
+        float* so = (l == J - 1) ? sJ : dst;
+        *reinterpret_cast<float4*>(so + i) = make_float4(s[0], s[1], s[2], s[3]);
+      };
+      const bool al = (((uintptr_t)dd_out | (uintptr_t)sJ | (uintptr_t)dst) & 15) == 0;
+      if (al && (l == 0 ? bfwd_level_vec<F, P, S>(x, N, 0, emitg)
+                        : bfwd_level_vec<F, P, V>((l & 1) ? tA : tB, N, l, emitg)))
+        continue;
+    }
     if (l == 0) bfwd_level_tiled<F, P, S>(x, N, 0, emit);
     else bfwd_level_tiled<F, P, V>((l & 1) ? tA : tB, N, l, emit);
   }
