@@ -294,6 +294,7 @@ def ours(args):
                 tiling[f"MODWT {FILTERS[f]}/{PREC[p]}"] = {
                     "fwd_target": mt[0], "fwd_smem_kb": mt[1], "inv_target": mt[2],
                     "inv_smem_kb": mt[3], "inv_levels": wc.get_modwt_inv_levels(f, p),
+                    "fwd_levels": wc.get_modwt_fwd_levels(f, p),
                     "fwd_ms": round(fms, 4), "inv_ms": round(ims, 4)}
 
     clocks = ClockSampler()
