@@ -1,4 +1,6 @@
 // Batched smoothing kernel, FP32 data and arithmetic (WC_F32).
+// Block-level MODWT tiles: 192 KB of shared memory per CTA (batch_kernel.cuh).
+#define WC_MOD_TILE_KB 192
 #include "batch_kernel.cuh"
 
 namespace wc {

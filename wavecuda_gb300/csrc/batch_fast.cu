@@ -1,4 +1,6 @@
 // Batched smoothing kernel, FP64 data with double-float arithmetic (WC_F64_FAST).
+// Block-level MODWT tiles: 192 KB of shared memory per CTA (batch_kernel.cuh).
+#define WC_MOD_TILE_KB 192
 #include "batch_kernel.cuh"
 
 namespace wc {

@@ -283,13 +283,21 @@ __device__ void bdwt_inv(const typename P::T* w, const D* coarse, D* out, int64_
 // ----------------------------------------------------- MODWT (block) ----
 // Stored coefficients: det = [d_1 | ... | d_J] (J blocks of N), sJ (N).
 
-// Shared-memory tiles of the block-level MODWT inverse: two stages of two
+// Shared-memory tiles of the block-level MODWT levels: two stages of two
 // arrays (scaling values, details) of mod_tile<V>() values each.  Kernels
-// that run it are launched with mod_tile_smem<V>() bytes of dynamic shared
-// memory (16 KB per array either way, 64 KB per CTA).
+// that run them are launched with mod_tile_smem<V>() bytes of dynamic shared
+// memory, WC_MOD_TILE_KB per CTA; each translation unit that instantiates a
+// kernel sets it for the CTAs it keeps per SM (the batched smoother runs one
+// 512-thread CTA per SM and takes 192 KB, the threshold tuner two 256-thread
+// CTAs and 104 KB each).  A tile's rows are a power of two, so three times
+// the memory gives four times the rows of a 32-column tile: a quarter of the
+// tile steps (two barriers each) and a smaller share of halo rows.
+#ifndef WC_MOD_TILE_KB
+#define WC_MOD_TILE_KB 64
+#endif
 template <class V>
 constexpr int mod_tile() {
-  return sizeof(V) == 8 ? 2048 : 4096;
+  return WC_MOD_TILE_KB * 1024 / (4 * (int)sizeof(V));
 }
 template <class V>
 constexpr size_t mod_tile_smem() {
@@ -480,109 +488,83 @@ __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, in
 template <int F, class P, class D, class TH>
 __device__ bool bmod_inv_level_vec(const void* S, bool top, const typename P::T* dl, int64_t N,
                                    int l, const TH& th, typename P::V* dst, D* out) {
-  using V = typename P::V;
-  using T = typename P::T;
-  constexpr int L = filter_len(F);
-  constexpr int W = mvec_w<P>();
-  constexpr int KT = mod_tile<V>();
-  constexpr bool kDD = std::is_same<P, PDD>::value;
   // FP32 only: in the exact and double-float batches, whose levels are
   // arithmetic-bound, these tiles measured 2-3 % slower than the one-value
   // level (4096-signal batch; FP32 9 % faster, the FP32 tuner 16 %).
-  if constexpr (!std::is_same<P, PF32>::value) return false;
-  const int64_t d0 = (int64_t)1 << l, rows = N >> l;
-  const int C = (int)(d0 < 32 ? d0 : 32);
-  const int HRp = mvec_inv_halo(L, 1, C, W);
-  int64_t M = rows;
-  while (M > 1 && (M + HRp) * C > KT) M >>= 1;
-  const bool last = (l == 0);
-  if (!mvec_ok(C, (int)M, W) || (M + HRp) * C > KT) return false;
-  if (((uintptr_t)S | (uintptr_t)dl | (uintptr_t)dst) & 15) return false;
-  if (last && (((uintptr_t)out & 15) || sizeof(D) != sizeof(T))) return false;
-  extern __shared__ __align__(16) unsigned char mod_smem[];
-  V* buf = reinterpret_cast<V*>(mod_smem);  // [stage][S | D][KT]
-  const int cs = __ffs(C) - 1;
-  const int64_t nb = d0 / C, ntiles = nb * (rows / M);
-  const int tot = (int)((M + HRp) * C), totc = tot / W;
-  const unsigned char* Sb = static_cast<const unsigned char*>(S);
-  auto issue = [&](int64_t tile, int stage) {
-    unsigned char* Ss = reinterpret_cast<unsigned char*>(buf + stage * 2 * KT);
-    unsigned char* Ds = Ss + KT * sizeof(V);
-    const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
-    for (int j = threadIdx.x; j < totc; j += blockDim.x) {
-      const int e = j * W;
-      const int row = e >> cs, c = e & (C - 1);
-      const int64_t g = (r0 + c) + ((m0 - HRp + row) & (rows - 1)) * d0;
-      cp_async16(Ss + (size_t)e * sizeof(V), Sb + (size_t)g * sizeof(V));
-      cp_async16(Ds + (size_t)e * sizeof(V), dl + g);
-    }
-    cp_async_commit();
-  };
-  issue(0, 0);
-  for (int64_t tile = 0; tile < ntiles; tile++) {
-    const int stage = (int)(tile & 1);
-    if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
-    else cp_async_commit();  // empty group keeps the wait count uniform
-    cp_async_wait_prior_1();
-    unsigned char* Ss = reinterpret_cast<unsigned char*>(buf + stage * 2 * KT);
-    unsigned char* Ds = Ss + KT * sizeof(V);
-    // Each thread converts (and thresholds) the chunks it copied.
-    for (int j = threadIdx.x; j < totc; j += blockDim.x) {
-      if constexpr (kDD) {
-        if (top) {
-          to_pair_chunk(Ss, j);
-        } else {
-          const float4 a = reinterpret_cast<const float4*>(Ss)[j];  // {hi0, lo0, hi1, lo1}
-          reinterpret_cast<PairChunk*>(Ss)[j] = PairChunk{x2_pack(a.x, a.z), x2_pack(a.y, a.w)};
-        }
-        const double2 v = reinterpret_cast<const double2*>(Ds)[j];
-        const dd a = thr_v<P>(dd_from_double(v.x), th, l), b = thr_v<P>(dd_from_double(v.y), th, l);
-        reinterpret_cast<PairChunk*>(Ds)[j] = PairChunk{x2_pack(a.hi, b.hi), x2_pack(a.lo, b.lo)};
-      } else {
+  if constexpr (!std::is_same<P, PF32>::value) {
+    return false;
+  } else {
+    using V = typename P::V;
+    using T = typename P::T;
+    constexpr int L = filter_len(F);
+    constexpr int W = mvec_w<P>();
+    constexpr int KT = mod_tile<V>();
+    const int64_t d0 = (int64_t)1 << l, rows = N >> l;
+    const int C = (int)(d0 < 32 ? d0 : 32);
+    const int HRp = mvec_inv_halo(L, 1, C, W);
+    int64_t M = rows;
+    while (M > 1 && (M + HRp) * C > KT) M >>= 1;
+    const bool last = (l == 0);
+    if (!mvec_ok(C, (int)M, W) || (M + HRp) * C > KT) return false;
+    if (((uintptr_t)S | (uintptr_t)dl | (uintptr_t)dst) & 15) return false;
+    if (last && (((uintptr_t)out & 15) || sizeof(D) != sizeof(T))) return false;
+    extern __shared__ __align__(16) unsigned char mod_smem[];
+    V* buf = reinterpret_cast<V*>(mod_smem);  // [stage][S | D][KT]
+    const int cs = __ffs(C) - 1;
+    const int64_t nb = d0 / C, ntiles = nb * (rows / M);
+    const int tot = (int)((M + HRp) * C), totc = tot / W;
+    const unsigned char* Sb = static_cast<const unsigned char*>(S);
+    auto issue = [&](int64_t tile, int stage) {
+      unsigned char* Ss = reinterpret_cast<unsigned char*>(buf + stage * 2 * KT);
+      unsigned char* Ds = Ss + KT * sizeof(V);
+      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+      for (int j = threadIdx.x; j < totc; j += blockDim.x) {
+        const int e = j * W;
+        const int row = e >> cs, c = e & (C - 1);
+        const int64_t g = (r0 + c) + ((m0 - HRp + row) & (rows - 1)) * d0;
+        cp_async16(Ss + (size_t)e * sizeof(V), Sb + (size_t)g * sizeof(V));
+        cp_async16(Ds + (size_t)e * sizeof(V), dl + g);
+      }
+      cp_async_commit();
+    };
+    issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+      const int stage = (int)(tile & 1);
+      if (tile + 1 < ntiles) issue(tile + 1, stage ^ 1);
+      else cp_async_commit();  // empty group keeps the wait count uniform
+      cp_async_wait_prior_1();
+      unsigned char* Ss = reinterpret_cast<unsigned char*>(buf + stage * 2 * KT);
+      unsigned char* Ds = Ss + KT * sizeof(V);
+      // Each thread converts (and thresholds) the chunks it copied.
+      for (int j = threadIdx.x; j < totc; j += blockDim.x) {
         Chunk<T> c = reinterpret_cast<const Chunk<T>*>(Ds)[j];
-#pragma unroll
+  #pragma unroll
         for (int i = 0; i < W; i++) c.v[i] = thr_v<P>(c.v[i], th, l);
         reinterpret_cast<Chunk<T>*>(Ds)[j] = c;
       }
-    }
-    __syncthreads();
-    const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
-    auto group = [&](auto rdc) {
-      constexpr int RD = decltype(rdc)::value;
-      for (int e = HRp * C + (int)threadIdx.x * W; e < tot; e += (int)blockDim.x * W) {
-        const int row = e >> cs, c = e & (C - 1);
-        const int64_t i = (r0 + c) + (m0 - HRp + row) * d0;
-        if constexpr (kDD) {
-          f32x2 hi, lo;
-          inv_group_dd<F, RD>(reinterpret_cast<const PairChunk*>(Ss),
-                              reinterpret_cast<const PairChunk*>(Ds), e, C, hi, lo);
-          float h0, h1, l0, l1;
-          x2_unpack(hi, h0, h1);
-          x2_unpack(lo, l0, l1);
-          if (last && !std::is_same<D, V>::value) {
-            *reinterpret_cast<double2*>(out + i) =
-                make_double2(dd_to_double(dd{h0, l0}), dd_to_double(dd{h1, l1}));
-          } else {
-            V* o = last ? reinterpret_cast<V*>(out) : dst;
-            *reinterpret_cast<float4*>(o + i) = make_float4(h0, l0, h1, l1);
-          }
-        } else {
+      __syncthreads();
+      const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
+      auto group = [&](auto rdc) {
+        constexpr int RD = decltype(rdc)::value;
+        for (int e = HRp * C + (int)threadIdx.x * W; e < tot; e += (int)blockDim.x * W) {
+          const int row = e >> cs, c = e & (C - 1);
+          const int64_t i = (r0 + c) + (m0 - HRp + row) * d0;
           V r[W];
-          inv_group<F, P, RD>(reinterpret_cast<const V*>(Ss), reinterpret_cast<const V*>(Ds), e,
-                              C, r);
+          inv_group<F, P, RD>(reinterpret_cast<const V*>(Ss), reinterpret_cast<const V*>(Ds), e, C,
+                              r);
           Chunk<T> ch;
-#pragma unroll
+  #pragma unroll
           for (int q = 0; q < W; q++) ch.v[q] = r[q];
           T* o = last ? reinterpret_cast<T*>(out) : reinterpret_cast<T*>(dst);
           *reinterpret_cast<Chunk<T>*>(o + i) = ch;
         }
-      }
-    };
-    if (C == 1) group(std::integral_constant<int, 1>{});
-    else group(std::integral_constant<int, 0>{});
-    __syncthreads();  // this stage is refilled two tiles later
+      };
+      if (C == 1) group(std::integral_constant<int, 1>{});
+      else group(std::integral_constant<int, 0>{});
+      __syncthreads();  // this stage is refilled two tiles later
+    }
+    return true;
   }
-  return true;
 }
 
 template <int F, class P, class D, class TH>

@@ -1,4 +1,6 @@
 // Batched threshold tuning kernel, FP32 data and arithmetic (WC_F32).
+// Block-level MODWT tiles: 104 KB of shared memory per CTA (batch_kernel.cuh).
+#define WC_MOD_TILE_KB 104
 #include "fit_kernel.cuh"
 
 namespace wc {

@@ -1,4 +1,6 @@
 // Batched threshold tuning kernel, FP64 data with double-float arithmetic (WC_F64_FAST).
+// Block-level MODWT tiles: 104 KB of shared memory per CTA (batch_kernel.cuh).
+#define WC_MOD_TILE_KB 104
 #include "fit_kernel.cuh"
 
 namespace wc {
