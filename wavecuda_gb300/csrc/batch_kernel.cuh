@@ -488,12 +488,11 @@ __device__ void bmodwt_fwd(const S* x, typename P::T* det, typename P::T* sJ, in
 template <int F, class P, class D, class TH>
 __device__ bool bmod_inv_level_vec(const void* S, bool top, const typename P::T* dl, int64_t N,
                                    int l, const TH& th, typename P::V* dst, D* out) {
-  // FP32 only: in the exact and double-float batches, whose levels are
-  // arithmetic-bound, these tiles measured 2-3 % slower than the one-value
-  // level (4096-signal batch; FP32 9 % faster, the FP32 tuner 16 %).
-  if constexpr (!std::is_same<P, PF32>::value) {
+  // Not in exact FP64, whose levels are bound by the FP64 pipe.
+  if constexpr (std::is_same<P, PExact>::value) {
     return false;
   } else {
+    constexpr bool kDD = std::is_same<P, PDD>::value;
     using V = typename P::V;
     using T = typename P::T;
     constexpr int L = filter_len(F);
@@ -537,10 +536,25 @@ __device__ bool bmod_inv_level_vec(const void* S, bool top, const typename P::T*
       unsigned char* Ds = Ss + KT * sizeof(V);
       // Each thread converts (and thresholds) the chunks it copied.
       for (int j = threadIdx.x; j < totc; j += blockDim.x) {
-        Chunk<T> c = reinterpret_cast<const Chunk<T>*>(Ds)[j];
-  #pragma unroll
-        for (int i = 0; i < W; i++) c.v[i] = thr_v<P>(c.v[i], th, l);
-        reinterpret_cast<Chunk<T>*>(Ds)[j] = c;
+        if constexpr (kDD) {
+          // pair chunks: scaling values from FP64 (top) or double-float
+          // {hi0, lo0, hi1, lo1}; details converted and thresholded
+          if (top) {
+            to_pair_chunk(Ss, j);
+          } else {
+            const float4 a = reinterpret_cast<const float4*>(Ss)[j];
+            reinterpret_cast<PairChunk*>(Ss)[j] = PairChunk{x2_pack(a.x, a.z), x2_pack(a.y, a.w)};
+          }
+          const double2 v = reinterpret_cast<const double2*>(Ds)[j];
+          const dd a = thr_v<P>(dd_from_double(v.x), th, l);
+          const dd b = thr_v<P>(dd_from_double(v.y), th, l);
+          reinterpret_cast<PairChunk*>(Ds)[j] = PairChunk{x2_pack(a.hi, b.hi), x2_pack(a.lo, b.lo)};
+        } else {
+          Chunk<T> c = reinterpret_cast<const Chunk<T>*>(Ds)[j];
+#pragma unroll
+          for (int i = 0; i < W; i++) c.v[i] = thr_v<P>(c.v[i], th, l);
+          reinterpret_cast<Chunk<T>*>(Ds)[j] = c;
+        }
       }
       __syncthreads();
       const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
@@ -549,14 +563,30 @@ __device__ bool bmod_inv_level_vec(const void* S, bool top, const typename P::T*
         for (int e = HRp * C + (int)threadIdx.x * W; e < tot; e += (int)blockDim.x * W) {
           const int row = e >> cs, c = e & (C - 1);
           const int64_t i = (r0 + c) + (m0 - HRp + row) * d0;
-          V r[W];
-          inv_group<F, P, RD>(reinterpret_cast<const V*>(Ss), reinterpret_cast<const V*>(Ds), e, C,
-                              r);
-          Chunk<T> ch;
-  #pragma unroll
-          for (int q = 0; q < W; q++) ch.v[q] = r[q];
-          T* o = last ? reinterpret_cast<T*>(out) : reinterpret_cast<T*>(dst);
-          *reinterpret_cast<Chunk<T>*>(o + i) = ch;
+          if constexpr (kDD) {
+            f32x2 hi, lo;
+            inv_group_dd<F, RD>(reinterpret_cast<const PairChunk*>(Ss),
+                                reinterpret_cast<const PairChunk*>(Ds), e, C, hi, lo);
+            float h0, h1, l0, l1;
+            x2_unpack(hi, h0, h1);
+            x2_unpack(lo, l0, l1);
+            if (last && !std::is_same<D, V>::value) {
+              *reinterpret_cast<double2*>(out + i) =
+                  make_double2(dd_to_double(dd{h0, l0}), dd_to_double(dd{h1, l1}));
+            } else {
+              V* o = last ? reinterpret_cast<V*>(out) : dst;
+              *reinterpret_cast<float4*>(o + i) = make_float4(h0, l0, h1, l1);
+            }
+          } else {
+            V r[W];
+            inv_group<F, P, RD>(reinterpret_cast<const V*>(Ss), reinterpret_cast<const V*>(Ds), e,
+                                C, r);
+            Chunk<T> ch;
+#pragma unroll
+            for (int q = 0; q < W; q++) ch.v[q] = r[q];
+            T* o = last ? reinterpret_cast<T*>(out) : reinterpret_cast<T*>(dst);
+            *reinterpret_cast<Chunk<T>*>(o + i) = ch;
+          }
         }
       };
       if (C == 1) group(std::integral_constant<int, 1>{});
