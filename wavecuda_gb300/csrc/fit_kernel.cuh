@@ -381,16 +381,35 @@ __device__ __noinline__ void fit_one(const FitArgs& a, int sig, CtaScratch cs, F
     if (!cv) {
       inv_any<F, P, V>(tt, c, cJ, (const V*)nullptr, fh, n, J, sh.th, tA, tB);
       float pl = 0.f;
-      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        float r;
-        if constexpr (std::is_same<V, dd>::value) {
-          const dd e = P::sub(fh[i], P::ld(xt[i]));
-          r = e.hi + e.lo;
-        } else {
-          r = vhi(fh[i]) - tf(xt[i]);
+      int64_t i0 = threadIdx.x;
+      if constexpr (std::is_same<P, PF32>::value) {
+        // four residuals per thread and step (scratch slices are 256-byte
+        // aligned); the last n % 4 one at a time below
+        float4* f4 = reinterpret_cast<float4*>(fh);
+        const float4* x4 = reinterpret_cast<const float4*>(xt);
+        for (int64_t i = threadIdx.x; i < n / 4; i += blockDim.x) {
+          const float4 a = f4[i], b = x4[i];
+          const float r0 = a.x - b.x, r1 = a.y - b.y, r2 = a.z - b.z, r3 = a.w - b.w;
+          pl += r0 * r0;
+          pl += r1 * r1;
+          pl += r2 * r2;
+          pl += r3 * r3;
+          f4[i] = make_float4(2.f * r0, 2.f * r1, 2.f * r2, 2.f * r3);
         }
-        pl += r * r;
-        fh[i] = from_f<V>(2.f * r);
+        i0 = (n / 4) * 4 + threadIdx.x;
+      }
+      {
+        for (int64_t i = i0; i < n; i += blockDim.x) {
+          float r;
+          if constexpr (std::is_same<V, dd>::value) {
+            const dd e = P::sub(fh[i], P::ld(xt[i]));
+            r = e.hi + e.lo;
+          } else {
+            r = vhi(fh[i]) - tf(xt[i]);
+          }
+          pl += r * r;
+          fh[i] = from_f<V>(2.f * r);
+        }
       }
       block_add(&sh.loss, pl);
       __syncthreads();
