@@ -1000,9 +1000,39 @@ __device__ dd bdd_reduce(dd v, SumShared& sh) {
 
 // Double-float sum of the loss terms j0 .. j1-1, in block order (the
 // precisions other than exact FP64; the result is valid in every thread).
+// FP32: each term from the FP32 reconstructions and the FP32 copy of the
+// signal xt in FP32 arithmetic (its rounding is that of the reconstructions
+// it is made of), added into a per-thread double-float sum; double-float:
+// every step in double-float from the FP64 signal xn.
 template <class P>
 __device__ dd bcv_part(const typename P::V* ye, const typename P::V* yo, const double* xn,
-                       int64_t lenh, int64_t j0, int64_t j1, SumShared& sh) {
+                       const typename P::T* xt, int64_t lenh, int64_t j0, int64_t j1,
+                       SumShared& sh) {
+  if constexpr (std::is_same<P, PF32>::value) {
+    float sh_ = 0.f, sl = 0.f;  // running double-float sum (hi, lo)
+    for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+      float yie, yio;
+      if (j == 0) {
+        yie = yo[0];
+        yio = 0.5f * (ye[0] + ye[1]);
+      } else if (j == lenh - 1) {
+        yio = ye[lenh - 1];
+        yie = 0.5f * (yo[j] + yo[j - 1]);
+      } else {
+        yio = 0.5f * (ye[j] + ye[j + 1]);
+        yie = 0.5f * (yo[j] + yo[j - 1]);
+      }
+      const float a = yie - xt[2 * j], b = yio - xt[2 * j + 1];
+      const float t = __fmaf_rn(a, a, b * b);
+      float s, e;
+      two_sum(sh_, t, s, e);
+      sh_ = s;
+      sl += e;
+    }
+    dd acc;
+    fast_two_sum(sh_, sl, acc.hi, acc.lo);
+    return bdd_reduce(acc, sh);
+  } else {
   const dd half{0.5f, 0.f};
   dd acc{0.f, 0.f};
   for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
@@ -1026,6 +1056,7 @@ __device__ dd bcv_part(const typename P::V* ye, const typename P::V* yo, const d
     acc = PDD::add(acc, PDD::add(dd_sqr(a), dd_sqr(b)));
   }
   return bdd_reduce(acc, sh);
+  }
 }
 
 // Sum of the interpolation loss terms (the quantity bcv_terms + bseq_sum
@@ -1035,13 +1066,13 @@ __device__ dd bcv_part(const typename P::V* ye, const typename P::V* yo, const d
 // (GB300's FP64 pipe is about 1/64 of its FP32 rate), in block order.
 template <class P>
 __device__ double bcv_sum(const typename P::V* ye, const typename P::V* yo, const double* xn,
-                          int64_t lenh, double* terms, SumShared& sh) {
+                          const typename P::T* xt, int64_t lenh, double* terms, SumShared& sh) {
   using V = typename P::V;
   if constexpr (std::is_same<P, PExact>::value) {
     bcv_terms<V>(ye, yo, xn, lenh, 0, lenh, terms);
     return bseq_sum(terms, lenh, sh);
   } else {
-    return dd_to_double(bcv_part<P>(ye, yo, xn, lenh, 0, lenh, sh));
+    return dd_to_double(bcv_part<P>(ye, yo, xn, xt, lenh, 0, lenh, sh));
   }
 }
 
@@ -1229,7 +1260,7 @@ __device__ bool cv_search(const BatchDesc& d, int role, BatchPair* pr, unsigned 
   auto loss = [&](int p) -> double {
     const V* ye = b.y[2 * p];
     const V* yo = b.y[2 * p + 1];
-    if (role == 0) return __dmul_rn(bcv_sum<P>(ye, yo, x, lenh, b.terms, sh.sum), 0.5);
+    if (role == 0) return __dmul_rn(bcv_sum<P>(ye, yo, x, b.xt, lenh, b.terms, sh.sum), 0.5);
     ok = pair_sync(pr, nb, status);  // both halves inverted
     if (!ok) return 0.0;
     const int64_t mid = lenh / 2;
@@ -1240,7 +1271,7 @@ __device__ bool cv_search(const BatchDesc& d, int role, BatchPair* pr, unsigned 
       if (!ok) return 0.0;
       return __dmul_rn(bseq_sum(b.terms, lenh, sh.sum), 0.5);
     } else {
-      const dd part = bcv_part<P>(ye, yo, x, lenh, j0, j1, sh.sum);
+      const dd part = bcv_part<P>(ye, yo, x, b.xt, lenh, j0, j1, sh.sum);
       if (threadIdx.x == 0) {
         pr->part[role - 1][0] = part.hi;
         pr->part[role - 1][1] = part.lo;
