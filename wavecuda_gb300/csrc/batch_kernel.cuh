@@ -560,6 +560,8 @@ __device__ bool bmod_inv_level_vec(const void* S, bool top, const typename P::T*
       const int64_t r0 = (tile % nb) * C, m0 = (tile / nb) * M;
       auto group = [&](auto rdc) {
         constexpr int RD = decltype(rdc)::value;
+        // FP32: two groups per thread in flight (double-float measured slower)
+#pragma unroll(kDD ? 1 : 2)
         for (int e = HRp * C + (int)threadIdx.x * W; e < tot; e += (int)blockDim.x * W) {
           const int row = e >> cs, c = e & (C - 1);
           const int64_t i = (r0 + c) + (m0 - HRp + row) * d0;
@@ -1010,6 +1012,7 @@ __device__ dd bcv_part(const typename P::V* ye, const typename P::V* yo, const d
                        SumShared& sh) {
   if constexpr (std::is_same<P, PF32>::value) {
     float sh_ = 0.f, sl = 0.f;  // running double-float sum (hi, lo)
+#pragma unroll 4
     for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
       float yie, yio;
       if (j == 0) {
