@@ -856,6 +856,19 @@ def profile_case(args):
         wc.smooth_batch(data, sigs, prec)
         print("ok", args.profile_case)
         return
+    if args.profile_case.startswith("batchcv:"):
+        # one batched-smoothing launch of 152 LA8 MODWT CV signals of
+        # 2^log2n (about 2 GB of scratch at 2^16): the batch's dominant kind
+        # of work, small enough for a multi-pass capture
+        from wavecuda_gb300 import signals as sg
+        prec = int(args.profile_case.split(":")[1])
+        m = 1 << args.log2n
+        data = np.concatenate([sg.noisy(sg.SHAPES["doppler"](m, i), 3.0, seed=i)
+                               for i in range(152)])
+        sigs = [wc.Signal(i * m, m, 10, 1, 4, 2, 1, 0, 9, 0.0, 1e-8) for i in range(152)]
+        wc.smooth_batch(data, sigs, prec)
+        print("ok", args.profile_case)
+        return
     kind, filt, prec = args.profile_case.split(":")
     filt, prec = int(filt), int(prec)
     es = 4 if prec == 2 else 8
@@ -906,7 +919,8 @@ def main():
     ap.add_argument("--cpu-log2n", type=int, default=24)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--profile-case", default=None,
-                    help="kind:filter:precision, e.g. dwt:2:1 -- one small case for ncu")
+                    help="kind:filter:precision, e.g. dwt:2:1, or batch:precision / "
+                         "batchcv:precision -- one small case for ncu")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
