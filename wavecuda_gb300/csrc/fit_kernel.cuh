@@ -398,18 +398,16 @@ __device__ __noinline__ void fit_one(const FitArgs& a, int sig, CtaScratch cs, F
         }
         i0 = (n / 4) * 4 + threadIdx.x;
       }
-      {
-        for (int64_t i = i0; i < n; i += blockDim.x) {
-          float r;
-          if constexpr (std::is_same<V, dd>::value) {
-            const dd e = P::sub(fh[i], P::ld(xt[i]));
-            r = e.hi + e.lo;
-          } else {
-            r = vhi(fh[i]) - tf(xt[i]);
-          }
-          pl += r * r;
-          fh[i] = from_f<V>(2.f * r);
+      for (int64_t i = i0; i < n; i += blockDim.x) {
+        float r;
+        if constexpr (std::is_same<V, dd>::value) {
+          const dd e = P::sub(fh[i], P::ld(xt[i]));
+          r = e.hi + e.lo;
+        } else {
+          r = vhi(fh[i]) - tf(xt[i]);
         }
+        pl += r * r;
+        fh[i] = from_f<V>(2.f * r);
       }
       block_add(&sh.loss, pl);
       __syncthreads();
